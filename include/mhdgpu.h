@@ -1,0 +1,186 @@
+/*
+ * mhdgpu.h - C ABI of the GB300 (sm_103a) implementation of one dimensionally
+ * split step of Pen's relaxing TVD MHD solver.
+ *
+ * Data layout (identical to the reference, Heterogeneous_MHD/C/array_definition.h:12-14):
+ *   u(5,nx,ny,nz) = (rho, m_x, m_y, m_z, E) and b(3,nx,ny,nz), FP32, component
+ *   fastest, then i, j, k.  b is face-centred on the left faces of each cell.
+ * Every subroutine works in the frame it is called with: the pencil runs along
+ * the first spatial axis (length nx), its neighbours are j+-1 and k+-1.
+ *
+ * Conventions of this ABI:
+ *   - plain pointers and sizes; device pointers unless a name says host;
+ *   - every entry returns an int status (MHD_OK on success) and never exits
+ *     or traps; mhdgpu_last_error() gives a message for the calling thread;
+ *   - the device entries are asynchronous on the given stream (NULL = legacy
+ *     default stream), allocate nothing and can be captured in a CUDA graph;
+ *   - the caller owns every buffer, scratch included (sizes from the
+ *     *_bytes queries); the library keeps no per-call state, so calls are
+ *     re-entrant on different streams.
+ *
+ * Citations are files of pandaPQY/MHD-GPU.
+ */
+#ifndef MHDGPU_H
+#define MHDGPU_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* cudaStream_t without including the CUDA headers */
+typedef struct CUstream_st *mhdgpu_stream_t;
+
+/* status codes */
+#define MHD_OK              0
+#define MHD_ERR_ARG         1   /* bad size, null pointer, aliasing, unsupported shape */
+#define MHD_ERR_CUDA        2   /* a CUDA runtime call failed */
+#define MHD_ERR_TIMEOUT     3   /* a bounded device wait gave up */
+#define MHD_ERR_UNPHYSICAL  4   /* the health word reports NaN/Inf, rho<=0 or p<=0 */
+#define MHD_ERR_NOMEM       5   /* a host-buffer entry could not allocate */
+
+/* CFL formulas */
+#define MHD_CFL_C           0   /* C path: the cell's own face B, unaveraged
+                                   (Heterogeneous_MHD/C/calcfl.c:13-65) */
+#define MHD_CFL_AVERAGED    1   /* release 0.2: B averaged to the cell centre
+                                   (OpenMP/mhd.f90:96-125, Cuda/cuda_cfl.cu:101-124) */
+
+/* device health word bits (OR-ed by the kernels, read by the host) */
+#define MHD_HEALTH_NONFINITE 1u  /* NaN or Inf in an updated state */
+#define MHD_HEALTH_DENSITY   2u  /* rho <= 0 */
+#define MHD_HEALTH_PRESSURE  4u  /* gas pressure <= 0 at the RK2 full step */
+
+/* largest pencil the device kernels accept (cells along the frame's x) */
+#define MHD_MAX_PENCIL      1024
+
+const char *mhdgpu_status_string(int status);
+const char *mhdgpu_last_error(void);
+const char *mhdgpu_version(void);
+
+/* ------------------------------------------------------------------------
+ * Per-subroutine device API.  These replace the reference CUDA wrappers of
+ * Heterogeneous_MHD/Cuda/cuda_subroutine.h:4-12 (which took the sizes both as
+ * host and device int* and synchronised after every call).
+ * ------------------------------------------------------------------------ */
+
+/* fluidx: relaxing-TVD RK2 update of u along the pencil with cell-centred B.
+ * Reads u_in and b (b at j+1 and k+1 for the transverse averages), writes
+ * u_out; u_out == u_in is allowed (in place).  dt is read from device memory.
+ * Replaces Cuda/cuda_fluidx.cu:12-23 and C/fluidx.c:19-102 (+ tvd1.c,
+ * mhdflux.c).  health may be NULL. */
+int mhdgpu_fluidx(float *u_out, const float *u_in, const float *b,
+                  int nx, int ny, int nz, const float *d_dt,
+                  unsigned *d_health, mhdgpu_stream_t stream);
+
+/* advectbyzx: constrained-transport advection of the two transverse face
+ * fields along the pencil, in place on b.  Needs caller scratch of
+ * mhdgpu_advectbyzx_scratch_bytes() (two floats per cell).
+ * Replaces Cuda/cuda_advectbyzx.cu:15-29 and C/advectbyzx.c:14-23
+ * (+ advectbyzxA1/A2/B1/B2.c, tvdb.c). */
+size_t mhdgpu_advectbyzx_scratch_bytes(int nx, int ny, int nz);
+int mhdgpu_advectbyzx(float *b, const float *u, int nx, int ny, int nz,
+                      const float *d_dt, float *d_scratch, mhdgpu_stream_t stream);
+
+/* transpose12: (nx,ny,nz) -> (ny,nx,nz), u components (1,3,2,4,5) and b
+ * components (2,1,3) (1-based).  Out of place; bit-exact.
+ * Replaces Cuda/cuda_transpose12.cu:12-38 and C/transpose12.c:7-47. */
+int mhdgpu_transpose12(float *dst_u, float *dst_b, const float *src_u, const float *src_b,
+                       int nx, int ny, int nz, mhdgpu_stream_t stream);
+
+/* transpose13: (nx,ny,nz) -> (nz,ny,nx), u components (1,4,3,2,5) and b
+ * components (3,2,1).  Out of place; bit-exact.  Unlike the reference
+ * (C/transpose13.c:16,58-61 refuses nx != nz) every shape is accepted.
+ * Replaces Cuda/cuda_transpose13.cu:14-55 and C/transpose13.c:9-62. */
+int mhdgpu_transpose13(float *dst_u, float *dst_b, const float *src_u, const float *src_b,
+                       int nx, int ny, int nz, mhdgpu_stream_t stream);
+
+/* cfl: writes 1/c_max to *d_inv_c, c_max = max over cells of the fast speed
+ * (mode MHD_CFL_C or MHD_CFL_AVERAGED).  d_scratch is one unsigned word.
+ * Replaces Cuda/cuda_cfl.cu:14-50 (whose result made a host round trip) and
+ * C/calcfl.c:13-65 (whose return value is 1/c). */
+int mhdgpu_cfl(const float *u, const float *b, int nx, int ny, int nz, int mode,
+               float *d_inv_c, unsigned *d_scratch, mhdgpu_stream_t stream);
+
+/* dt update of the driver (C/mhd.c:63-65) on the device:
+ *   dt = (float)(cfl_number * (double)inv_c); if tf > 0 and dt > (tf - t)/2
+ *   then dt = (tf - t)/2; t = t + 2*dt.  tf <= 0 disables the clamp. */
+int mhdgpu_dt_update(const float *d_inv_c, double cfl_number, float tf,
+                     float *d_t, float *d_dt, mhdgpu_stream_t stream);
+
+/* copy_matrix (C/copy_matrix.c:9-38): update <- (u, b). */
+int mhdgpu_copy_matrix(float *dst_u, float *dst_b, const float *src_u, const float *src_b,
+                       int nx, int ny, int nz, mhdgpu_stream_t stream);
+
+/* ------------------------------------------------------------------------
+ * Whole step.  The sequence is the reference's Strang-symmetric
+ * x, y(T12), z(T13), z, y(T13), x(T12) (C/mhd.c:72-119) built from the
+ * per-subroutine kernels above, with the transposes ping-ponging between the
+ * state and the workspace instead of the reference's copy_matrix calls.
+ * ------------------------------------------------------------------------ */
+
+/* workspace for mhdgpu_step / mhdgpu_advance (40 bytes per cell) */
+size_t mhdgpu_step_workspace_bytes(int nx, int ny, int nz);
+
+/* one full step at the dt held in *d_dt, in place on (u, b) */
+int mhdgpu_step(float *u, float *b, int nx, int ny, int nz, const float *d_dt,
+                void *d_work, unsigned *d_health, mhdgpu_stream_t stream);
+
+/* clock of a run kept on the device */
+typedef struct {
+    float t;        /* simulation time */
+    float dt;       /* dt of the last step */
+    float inv_c;    /* 1/c_max of the last CFL evaluation */
+    unsigned cmax;  /* CFL reduction word (kept at 0 between steps) */
+    unsigned health;/* MHD_HEALTH_* bits */
+    int iter;       /* steps taken */
+} mhdgpu_clock;
+
+/* nsteps iterations of: CFL -> dt update -> step, all on the device
+ * (C/mhd.c:60-125 without its printfs).  d_dt_log (may be NULL) receives each
+ * step's dt at d_dt_log[clock.iter].  Steps with tf > 0 and t >= tf are
+ * skipped on the device (the reference's do-while exit). */
+int mhdgpu_advance(float *u, float *b, int nx, int ny, int nz, int nsteps,
+                   double cfl_number, int cfl_mode, float tf,
+                   mhdgpu_clock *d_clock, float *d_dt_log, void *d_work,
+                   mhdgpu_stream_t stream);
+
+/* ------------------------------------------------------------------------
+ * Host-buffer entry (the end-to-end path): uploads (u, b) from host memory,
+ * runs up to max_steps steps as mhdgpu_advance does, downloads the state.
+ * Allocates its device buffers per call.  *t is read and updated; dt_log may
+ * be NULL.  Returns the steps taken in *steps_done (may be NULL).
+ * ------------------------------------------------------------------------ */
+int mhdgpu_run_host(float *u, float *b, int nx, int ny, int nz, double cfl_number,
+                    int cfl_mode, float *t, float tf, int max_steps, float *dt_log,
+                    int *steps_done);
+
+/* ------------------------------------------------------------------------
+ * Profiler: per-kernel-class device time from CUDA events.  While a profiler
+ * is attached to the calling thread, every entry above records a start and
+ * an end event on its stream around its launches (no added synchronisation;
+ * not for use under stream capture).  The reference timed whole steps only
+ * (Cuda/cuda_main.cu:68-77,122-128).
+ * ------------------------------------------------------------------------ */
+#define MHD_KCLASS_FLUIDX     0   /* fluidx kernel */
+#define MHD_KCLASS_ADVECT     1   /* advectbyzx flux kernel + b_x gather kernel */
+#define MHD_KCLASS_TRANSPOSE  2   /* transpose12 / transpose13 */
+#define MHD_KCLASS_CFL        3   /* CFL reduction (+ its clock/finish kernel) */
+#define MHD_KCLASS_COUNT      4
+
+typedef struct mhdgpu_profiler mhdgpu_profiler;
+int mhdgpu_profiler_create(mhdgpu_profiler **p, int max_records);
+int mhdgpu_profiler_destroy(mhdgpu_profiler *p);
+/* attach to the calling thread; NULL detaches */
+int mhdgpu_profiler_attach(mhdgpu_profiler *p);
+int mhdgpu_profiler_reset(mhdgpu_profiler *p);
+/* waits for the recorded events of one class; records = timed regions,
+ * launches = kernels launched inside them, total_ms = summed device time */
+int mhdgpu_profiler_summary(mhdgpu_profiler *p, int kclass, int *records, int *launches,
+                            double *total_ms);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MHDGPU_H */

@@ -1,0 +1,304 @@
+// capi.cu - the C ABI of include/mhdgpu.h: argument checks, status codes and
+// the step driver that sequences the per-subroutine kernels.
+//
+// The step driver restates the reference's sweep order
+// (Heterogeneous_MHD/C/mhd.c:72-119): x, then y after transpose12, z twice
+// after transpose13, y after transpose13, x after transpose12, with the
+// fluid/field order reversed on the way back.  The reference copies the whole
+// state after every subroutine (copy_matrix, 16 per step); here fluidx and
+// advectbyzx run in place and only the transposes move data, ping-ponging
+// between the caller's state and the workspace.
+#include <cuda_runtime.h>
+#include <stdio.h>
+#include <string.h>
+
+#include "kernels.cuh"
+#include "profiler.cuh"
+
+using namespace mhd;
+
+static thread_local char g_err[512];
+
+static int fail(int status, const char *fmt, const char *detail = nullptr)
+{
+    if (detail) snprintf(g_err, sizeof g_err, fmt, detail);
+    else snprintf(g_err, sizeof g_err, "%s", fmt);
+    return status;
+}
+
+static int cuda_fail(cudaError_t e, const char *where)
+{
+    snprintf(g_err, sizeof g_err, "%s: %s", where, cudaGetErrorString(e));
+    return MHD_ERR_CUDA;
+}
+
+#define MHD_CU(call, where)                              \
+    do {                                                 \
+        cudaError_t e_ = (call);                         \
+        if (e_ != cudaSuccess) return cuda_fail(e_, where); \
+    } while (0)
+
+static bool dims_ok(int nx, int ny, int nz)
+{
+    if (nx < 1 || ny < 1 || nz < 1) return false;
+    if (nx > MHD_MAX_PENCIL) return false;
+    const long long ncell = (long long)nx * ny * nz;
+    return ncell <= (1LL << 31) / 8;   // 8 floats per cell addressable with int offsets
+}
+
+static int check_dims(int nx, int ny, int nz, const char *who)
+{
+    if (!dims_ok(nx, ny, nz)) {
+        snprintf(g_err, sizeof g_err, "%s: bad box %dx%dx%d (each >= 1, nx <= %d, <= 2^28 cells)",
+                 who, nx, ny, nz, MHD_MAX_PENCIL);
+        return MHD_ERR_ARG;
+    }
+    return MHD_OK;
+}
+
+extern "C" {
+
+const char *mhdgpu_status_string(int status)
+{
+    switch (status) {
+    case MHD_OK: return "ok";
+    case MHD_ERR_ARG: return "invalid argument";
+    case MHD_ERR_CUDA: return "CUDA error";
+    case MHD_ERR_TIMEOUT: return "device wait timed out";
+    case MHD_ERR_UNPHYSICAL: return "unphysical state";
+    case MHD_ERR_NOMEM: return "out of memory";
+    default: return "unknown status";
+    }
+}
+
+const char *mhdgpu_last_error(void) { return g_err; }
+
+const char *mhdgpu_version(void) { return "mhdgpu 0.1 sm_103a"; }
+
+int mhdgpu_fluidx(float *u_out, const float *u_in, const float *b, int nx, int ny, int nz,
+                  const float *d_dt, unsigned *d_health, mhdgpu_stream_t stream)
+{
+    int st = check_dims(nx, ny, nz, "mhdgpu_fluidx");
+    if (st) return st;
+    if (!u_out || !u_in || !b || !d_dt) return fail(MHD_ERR_ARG, "mhdgpu_fluidx: null pointer");
+    const long long n5 = 5LL * nx * ny * nz;
+    if (u_out != u_in && u_out < u_in + n5 && u_in < u_out + n5)
+        return fail(MHD_ERR_ARG, "mhdgpu_fluidx: u_out partially overlaps u_in");
+    FluidxArgs a{u_out, u_in, b, d_dt, d_health, make_frame(nx, ny, nz)};
+    ProfScope ps(MHD_KCLASS_FLUIDX, 1, (cudaStream_t)stream);
+    MHD_CU(launch_fluidx(a, fluidx_pick(nx), (cudaStream_t)stream), "mhdgpu_fluidx");
+    return MHD_OK;
+}
+
+size_t mhdgpu_advectbyzx_scratch_bytes(int nx, int ny, int nz)
+{
+    if (!dims_ok(nx, ny, nz)) return 0;
+    return sizeof(float) * 2 * (size_t)nx * ny * nz;
+}
+
+int mhdgpu_advectbyzx(float *b, const float *u, int nx, int ny, int nz, const float *d_dt,
+                      float *d_scratch, mhdgpu_stream_t stream)
+{
+    int st = check_dims(nx, ny, nz, "mhdgpu_advectbyzx");
+    if (st) return st;
+    if (!b || !u || !d_dt || !d_scratch) return fail(MHD_ERR_ARG, "mhdgpu_advectbyzx: null pointer");
+    const long long ncell = (long long)nx * ny * nz;
+    AdvectArgs a{b, u, d_dt, d_scratch, d_scratch + ncell, make_frame(nx, ny, nz)};
+    ProfScope ps(MHD_KCLASS_ADVECT, 2, (cudaStream_t)stream);
+    MHD_CU(launch_advect(a, advect_pick(nx), (cudaStream_t)stream), "mhdgpu_advectbyzx");
+    return MHD_OK;
+}
+
+static int transpose_common(float *dst_u, float *dst_b, const float *src_u, const float *src_b,
+                            int nx, int ny, int nz, int which, mhdgpu_stream_t stream)
+{
+    const char *who = which == 12 ? "mhdgpu_transpose12" : "mhdgpu_transpose13";
+    if (nx < 1 || ny < 1 || nz < 1 || (long long)nx * ny * nz > (1LL << 28))
+        return fail(MHD_ERR_ARG, "%s: bad box", who);
+    if (!dst_u || !dst_b || !src_u || !src_b) return fail(MHD_ERR_ARG, "%s: null pointer", who);
+    if (dst_u == src_u || dst_b == src_b) return fail(MHD_ERR_ARG, "%s: transposes are out of place", who);
+    if ((which == 12 ? nz : ny) > 65535) return fail(MHD_ERR_ARG, "%s: outer extent above 65535", who);
+    ProfScope ps(MHD_KCLASS_TRANSPOSE, 1, (cudaStream_t)stream);
+    MHD_CU(launch_transpose(dst_u, dst_b, src_u, src_b, nx, ny, nz, which, (cudaStream_t)stream), who);
+    return MHD_OK;
+}
+
+int mhdgpu_transpose12(float *dst_u, float *dst_b, const float *src_u, const float *src_b,
+                       int nx, int ny, int nz, mhdgpu_stream_t stream)
+{
+    return transpose_common(dst_u, dst_b, src_u, src_b, nx, ny, nz, 12, stream);
+}
+
+int mhdgpu_transpose13(float *dst_u, float *dst_b, const float *src_u, const float *src_b,
+                       int nx, int ny, int nz, mhdgpu_stream_t stream)
+{
+    return transpose_common(dst_u, dst_b, src_u, src_b, nx, ny, nz, 13, stream);
+}
+
+int mhdgpu_cfl(const float *u, const float *b, int nx, int ny, int nz, int mode, float *d_inv_c,
+               unsigned *d_scratch, mhdgpu_stream_t stream)
+{
+    if (nx < 1 || ny < 1 || nz < 1 || (long long)nx * ny * nz > (1LL << 28))
+        return fail(MHD_ERR_ARG, "mhdgpu_cfl: bad box");
+    if (!u || !b || !d_inv_c || !d_scratch) return fail(MHD_ERR_ARG, "mhdgpu_cfl: null pointer");
+    if (mode != MHD_CFL_C && mode != MHD_CFL_AVERAGED) return fail(MHD_ERR_ARG, "mhdgpu_cfl: bad mode");
+    cudaStream_t s = (cudaStream_t)stream;
+    MHD_CU(cudaMemsetAsync(d_scratch, 0, sizeof(unsigned), s), "mhdgpu_cfl");
+    ProfScope ps(MHD_KCLASS_CFL, 2, s);
+    MHD_CU(launch_cfl(u, b, nx, ny, nz, mode, d_scratch, s), "mhdgpu_cfl");
+    MHD_CU(launch_cfl_finish(d_scratch, d_inv_c, s), "mhdgpu_cfl");
+    return MHD_OK;
+}
+
+int mhdgpu_dt_update(const float *d_inv_c, double cfl_number, float tf, float *d_t, float *d_dt,
+                     mhdgpu_stream_t stream)
+{
+    if (!d_inv_c || !d_t || !d_dt) return fail(MHD_ERR_ARG, "mhdgpu_dt_update: null pointer");
+    if (!(cfl_number > 0.0)) return fail(MHD_ERR_ARG, "mhdgpu_dt_update: cfl_number must be > 0");
+    MHD_CU(launch_dt_update(d_inv_c, cfl_number, tf, d_t, d_dt, (cudaStream_t)stream), "mhdgpu_dt_update");
+    return MHD_OK;
+}
+
+int mhdgpu_copy_matrix(float *dst_u, float *dst_b, const float *src_u, const float *src_b,
+                       int nx, int ny, int nz, mhdgpu_stream_t stream)
+{
+    if (nx < 1 || ny < 1 || nz < 1) return fail(MHD_ERR_ARG, "mhdgpu_copy_matrix: bad box");
+    if (!dst_u || !dst_b || !src_u || !src_b) return fail(MHD_ERR_ARG, "mhdgpu_copy_matrix: null pointer");
+    const size_t ncell = (size_t)nx * ny * nz;
+    cudaStream_t s = (cudaStream_t)stream;
+    MHD_CU(cudaMemcpyAsync(dst_u, src_u, ncell * 5 * sizeof(float), cudaMemcpyDeviceToDevice, s),
+           "mhdgpu_copy_matrix");
+    MHD_CU(cudaMemcpyAsync(dst_b, src_b, ncell * 3 * sizeof(float), cudaMemcpyDeviceToDevice, s),
+           "mhdgpu_copy_matrix");
+    return MHD_OK;
+}
+
+size_t mhdgpu_step_workspace_bytes(int nx, int ny, int nz)
+{
+    if (!dims_ok(nx, ny, nz) || ny > MHD_MAX_PENCIL || nz > MHD_MAX_PENCIL) return 0;
+    return sizeof(float) * 10 * (size_t)nx * ny * nz;
+}
+
+// one sweep pair in frame (n, a, c): fluid then field, or field then fluid
+static int sweep(float *u, float *b, int n, int a, int c, const float *dt, float *scr,
+                 unsigned *health, bool fluid_first, cudaStream_t s)
+{
+    int st;
+    if (fluid_first) {
+        if ((st = mhdgpu_fluidx(u, u, b, n, a, c, dt, health, (mhdgpu_stream_t)s))) return st;
+        return mhdgpu_advectbyzx(b, u, n, a, c, dt, scr, (mhdgpu_stream_t)s);
+    }
+    if ((st = mhdgpu_advectbyzx(b, u, n, a, c, dt, scr, (mhdgpu_stream_t)s))) return st;
+    return mhdgpu_fluidx(u, u, b, n, a, c, dt, health, (mhdgpu_stream_t)s);
+}
+
+int mhdgpu_step(float *u, float *b, int nx, int ny, int nz, const float *d_dt, void *d_work,
+                unsigned *d_health, mhdgpu_stream_t stream)
+{
+    int st = check_dims(nx, ny, nz, "mhdgpu_step");
+    if (st) return st;
+    if (ny > MHD_MAX_PENCIL || nz > MHD_MAX_PENCIL)
+        return fail(MHD_ERR_ARG, "mhdgpu_step: every axis becomes a pencil; each must be <= MHD_MAX_PENCIL");
+    if (!u || !b || !d_dt || !d_work) return fail(MHD_ERR_ARG, "mhdgpu_step: null pointer");
+    cudaStream_t s = (cudaStream_t)stream;
+    const size_t ncell = (size_t)nx * ny * nz;
+    float *u2 = (float *)d_work;
+    float *b2 = u2 + 5 * ncell;
+    float *scr = b2 + 3 * ncell;
+    // x
+    if ((st = sweep(u, b, nx, ny, nz, d_dt, scr, d_health, true, s))) return st;
+    // y (frame ny, nx, nz)
+    if ((st = mhdgpu_transpose12(u2, b2, u, b, nx, ny, nz, stream))) return st;
+    if ((st = sweep(u2, b2, ny, nx, nz, d_dt, scr, d_health, true, s))) return st;
+    // z twice (frame nz, nx, ny)
+    if ((st = mhdgpu_transpose13(u, b, u2, b2, ny, nx, nz, stream))) return st;
+    if ((st = sweep(u, b, nz, nx, ny, d_dt, scr, d_health, true, s))) return st;
+    if ((st = sweep(u, b, nz, nx, ny, d_dt, scr, d_health, false, s))) return st;
+    // y back (frame ny, nx, nz)
+    if ((st = mhdgpu_transpose13(u2, b2, u, b, nz, nx, ny, stream))) return st;
+    if ((st = sweep(u2, b2, ny, nx, nz, d_dt, scr, d_health, false, s))) return st;
+    // x back
+    if ((st = mhdgpu_transpose12(u, b, u2, b2, ny, nx, nz, stream))) return st;
+    return sweep(u, b, nx, ny, nz, d_dt, scr, d_health, false, s);
+}
+
+int mhdgpu_advance(float *u, float *b, int nx, int ny, int nz, int nsteps, double cfl_number,
+                   int cfl_mode, float tf, mhdgpu_clock *d_clock, float *d_dt_log, void *d_work,
+                   mhdgpu_stream_t stream)
+{
+    if (nsteps < 0) return fail(MHD_ERR_ARG, "mhdgpu_advance: nsteps < 0");
+    if (!d_clock) return fail(MHD_ERR_ARG, "mhdgpu_advance: null clock");
+    if (!(cfl_number > 0.0)) return fail(MHD_ERR_ARG, "mhdgpu_advance: cfl_number must be > 0");
+    if (cfl_mode != MHD_CFL_C && cfl_mode != MHD_CFL_AVERAGED)
+        return fail(MHD_ERR_ARG, "mhdgpu_advance: bad cfl mode");
+    cudaStream_t s = (cudaStream_t)stream;
+    for (int it = 0; it < nsteps; ++it) {
+        {
+            ProfScope ps(MHD_KCLASS_CFL, 2, s);
+            MHD_CU(launch_cfl(u, b, nx, ny, nz, cfl_mode, &d_clock->cmax, s), "mhdgpu_advance");
+            MHD_CU(launch_clock(d_clock, cfl_number, tf, d_dt_log, s), "mhdgpu_advance");
+        }
+        int st = mhdgpu_step(u, b, nx, ny, nz, &d_clock->dt, d_work, &d_clock->health, stream);
+        if (st) return st;
+    }
+    return MHD_OK;
+}
+
+int mhdgpu_run_host(float *u, float *b, int nx, int ny, int nz, double cfl_number, int cfl_mode,
+                    float *t, float tf, int max_steps, float *dt_log, int *steps_done)
+{
+    int st = check_dims(nx, ny, nz, "mhdgpu_run_host");
+    if (st) return st;
+    if (!u || !b || !t) return fail(MHD_ERR_ARG, "mhdgpu_run_host: null pointer");
+    if (max_steps < 0) return fail(MHD_ERR_ARG, "mhdgpu_run_host: max_steps < 0");
+    const size_t ncell = (size_t)nx * ny * nz;
+    const size_t wbytes = mhdgpu_step_workspace_bytes(nx, ny, nz);
+    if (!wbytes) return fail(MHD_ERR_ARG, "mhdgpu_run_host: box too large for the step");
+    float *du = nullptr, *db = nullptr, *dlog = nullptr;
+    void *dw = nullptr;
+    mhdgpu_clock *dclk = nullptr;
+    cudaStream_t s = nullptr;
+    int ret = MHD_OK;
+    cudaError_t e;
+#define RH(call, where) do { e = (call); if (e != cudaSuccess) { ret = cuda_fail(e, where); goto done; } } while (0)
+    RH(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), "mhdgpu_run_host: stream");
+    RH(cudaMallocAsync((void **)&du, ncell * 5 * sizeof(float), s), "mhdgpu_run_host: alloc");
+    RH(cudaMallocAsync((void **)&db, ncell * 3 * sizeof(float), s), "mhdgpu_run_host: alloc");
+    RH(cudaMallocAsync(&dw, wbytes, s), "mhdgpu_run_host: alloc");
+    RH(cudaMallocAsync((void **)&dclk, sizeof(mhdgpu_clock), s), "mhdgpu_run_host: alloc");
+    RH(cudaMallocAsync((void **)&dlog, sizeof(float) * (max_steps > 0 ? max_steps : 1), s), "mhdgpu_run_host: alloc");
+    {
+        mhdgpu_clock h;
+        memset(&h, 0, sizeof h);
+        h.t = *t;
+        RH(cudaMemcpyAsync(dclk, &h, sizeof h, cudaMemcpyHostToDevice, s), "mhdgpu_run_host: upload");
+        RH(cudaMemcpyAsync(du, u, ncell * 5 * sizeof(float), cudaMemcpyHostToDevice, s), "mhdgpu_run_host: upload");
+        RH(cudaMemcpyAsync(db, b, ncell * 3 * sizeof(float), cudaMemcpyHostToDevice, s), "mhdgpu_run_host: upload");
+        ret = mhdgpu_advance(du, db, nx, ny, nz, max_steps, cfl_number, cfl_mode, tf, dclk, dlog, dw,
+                             (mhdgpu_stream_t)s);
+        if (ret) goto done;
+        RH(cudaMemcpyAsync(u, du, ncell * 5 * sizeof(float), cudaMemcpyDeviceToHost, s), "mhdgpu_run_host: download");
+        RH(cudaMemcpyAsync(b, db, ncell * 3 * sizeof(float), cudaMemcpyDeviceToHost, s), "mhdgpu_run_host: download");
+        RH(cudaMemcpyAsync(&h, dclk, sizeof h, cudaMemcpyDeviceToHost, s), "mhdgpu_run_host: download");
+        RH(cudaStreamSynchronize(s), "mhdgpu_run_host: sync");
+        if (dt_log && h.iter > 0)
+            RH(cudaMemcpy(dt_log, dlog, sizeof(float) * h.iter, cudaMemcpyDeviceToHost), "mhdgpu_run_host: dt log");
+        *t = h.t;
+        if (steps_done) *steps_done = h.iter;
+        if (h.health) ret = fail(MHD_ERR_UNPHYSICAL, "mhdgpu_run_host: health word set (NaN/Inf, rho<=0 or p<=0)");
+    }
+done:
+    if (s) {
+        cudaFreeAsync(du, s);
+        cudaFreeAsync(db, s);
+        cudaFreeAsync(dw, s);
+        cudaFreeAsync(dclk, s);
+        cudaFreeAsync(dlog, s);
+        cudaStreamSynchronize(s);
+        cudaStreamDestroy(s);
+    }
+#undef RH
+    return ret;
+}
+
+}  // extern "C"

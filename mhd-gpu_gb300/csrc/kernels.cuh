@@ -1,0 +1,47 @@
+// kernels.cuh - argument blocks and launchers shared by the kernel files and
+// the C ABI (capi.cu).  Private to the library.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "mhd_common.cuh"
+
+namespace mhd {
+
+struct FluidxArgs {
+    float *u_out;
+    const float *u_in;
+    const float *b;
+    const float *dt;
+    unsigned *health;
+    Frame f;
+};
+
+struct AdvectArgs {
+    float *b;             // in place (b_y, b_z by the flux kernel, b_x by the gather)
+    const float *u;
+    const float *dt;
+    float *sA;            // ncell: shifted stage-A flux
+    float *sB;            // ncell: shifted stage-B flux
+    Frame f;
+};
+
+// team shape of the pencil kernels: CPL cells per thread, WPP warps per
+// pencil, PPC pencils per CTA
+struct PencilCfg { int cpl, wpp, ppc; };
+
+PencilCfg fluidx_pick(int n);
+PencilCfg advect_pick(int n);
+cudaError_t launch_fluidx(const FluidxArgs &a, const PencilCfg &cfg, cudaStream_t s);
+cudaError_t launch_advect(const AdvectArgs &a, const PencilCfg &cfg, cudaStream_t s);
+cudaError_t launch_transpose(float *du, float *db, const float *su, const float *sb,
+                             int nx, int ny, int nz, int which, cudaStream_t s);
+cudaError_t launch_cfl(const float *u, const float *b, int nx, int ny, int nz, int mode,
+                       unsigned *cmax, cudaStream_t s);
+cudaError_t launch_cfl_finish(unsigned *cmax, float *inv_c, cudaStream_t s);
+cudaError_t launch_dt_update(const float *inv_c, double cfl_number, float tf, float *t, float *dt,
+                             cudaStream_t s);
+cudaError_t launch_clock(mhdgpu_clock *clk, double cfl_number, float tf, float *dt_log,
+                         cudaStream_t s);
+
+}  // namespace mhd

@@ -1,0 +1,128 @@
+"""Initial states for the MHD step, in the reference layout.
+
+u(5,nx,ny,nz) = (rho, m_x, m_y, m_z, E) and b(3,nx,ny,nz) face-centred on the
+left faces, component fastest then i, j, k (Heterogeneous_MHD/C/array_definition.h:12-14).
+All generators return flat float32 (or float64) numpy arrays ``(u, b)``.
+
+The box has unit cell size, L = n along each axis, as in the reference driver
+(tf = 4*nx, Heterogeneous_MHD/C/mhd.c:59).  E is built with the same face->centre
+average of B that fluidx applies (Heterogeneous_MHD/C/fluidx.c:71-81), so a
+uniform state is in discrete equilibrium.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+GAMMA = 5.0 / 3.0
+
+
+def _pack(rho, m, e, b, dtype):
+    """rho,e: (nz,ny,nx); m,b: (3,nz,ny,nx) -> flat AoS u, b."""
+    nz, ny, nx = rho.shape
+    u = np.empty((nz, ny, nx, 5), dtype=np.float64)
+    u[..., 0] = rho
+    u[..., 1:4] = np.moveaxis(m, 0, -1)
+    u[..., 4] = e
+    bb = np.moveaxis(b, 0, -1)
+    return (np.ascontiguousarray(u.astype(dtype)).ravel(),
+            np.ascontiguousarray(bb.astype(dtype)).ravel())
+
+
+def centred_b(b):
+    """Face (left) -> cell centre average, b: (3,nz,ny,nx)."""
+    return np.stack([(b[0] + np.roll(b[0], -1, axis=2)) / 2,
+                     (b[1] + np.roll(b[1], -1, axis=1)) / 2,
+                     (b[2] + np.roll(b[2], -1, axis=0)) / 2])
+
+
+def _energy(rho, m, b, p):
+    bc = centred_b(b)
+    return p / (GAMMA - 1.0) + 0.5 * (m ** 2).sum(0) / rho + 0.5 * (bc ** 2).sum(0)
+
+
+def alfven_x(n=32, amp=1e-3, rho0=1.0, p0=1.0, dtype=np.float32, ny=None, nz=None):
+    """Linear Alfven wave along x on B0=(1,0,0): dv_y = A cos(2 pi x/L),
+    dB_y = -A sqrt(rho) cos(2 pi x/L), x at cell centres (i+1/2).  b_y sits on
+    y-faces at the x cell centre, so it is divergence-free exactly."""
+    nx = n
+    ny = n if ny is None else ny
+    nz = n if nz is None else nz
+    x = (np.arange(nx) + 0.5)
+    ph = np.cos(2 * np.pi * x / nx)[None, None, :] * np.ones((nz, ny, 1))
+    rho = np.full((nz, ny, nx), rho0)
+    m = np.zeros((3, nz, ny, nx))
+    m[1] = rho * amp * ph
+    b = np.zeros((3, nz, ny, nx))
+    b[0] = 1.0
+    b[1] = -amp * np.sqrt(rho0) * ph
+    e = _energy(rho, m, b, p0)
+    return _pack(rho, m, e, b, dtype)
+
+
+def _edge_potential_curl(ax, ay, az):
+    """Discrete curl of an edge-centred vector potential onto left faces.
+
+    A_x lives at (i+1/2, j, k), A_y at (i, j+1/2, k), A_z at (i, j, k+1/2)
+    (arrays indexed [k, j, i]); b_x at (i, j+1/2, k+1/2) etc.  The result has
+    zero discrete divergence b1(i+1)-b1(i)+b2(j+1)-b2(j)+b3(k+1)-b3(k)."""
+    dyz = lambda a, axis: np.roll(a, -1, axis=axis) - a
+    bx = dyz(az, 1) - dyz(ay, 0)
+    by = dyz(ax, 0) - dyz(az, 2)
+    bz = dyz(ay, 2) - dyz(ax, 1)
+    return np.stack([bx, by, bz])
+
+
+def alfven_oblique(n=128, kvec=(1, 1, 1), amp=1e-3, rho0=1.0, p0=1.0, dtype=np.float32):
+    """Linear Alfven wave with wave vector k = kvec 2pi/L and B0 = khat.
+
+    The perturbation direction is e1 = normalised (khat x z) (or khat x x when
+    khat is parallel to z); dv = A cos(k.x) e1 at cell centres and
+    dB = -A sqrt(rho) cos(k.x) e1 from a staggered vector potential, so the
+    face field is divergence-free to round-off."""
+    nx = ny = nz = n
+    kv = np.asarray(kvec, dtype=np.float64) * 2 * np.pi / n
+    kh = kv / np.linalg.norm(kv)
+    ref = np.array([0.0, 0.0, 1.0]) if abs(kh[2]) < 0.9 else np.array([1.0, 0.0, 0.0])
+    e1 = np.cross(kh, ref)
+    e1 /= np.linalg.norm(e1)
+    kk, jj, ii = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
+
+    def phase(ox, oy, oz):
+        return kv[0] * (ii + ox) + kv[1] * (jj + oy) + kv[2] * (kk + oz)
+
+    rho = np.full((nz, ny, nx), rho0)
+    m = rho * amp * np.cos(phase(0.5, 0.5, 0.5))[None] * e1[:, None, None, None]
+    # dB = -amp*sqrt(rho)*cos(k.x) e1 = curl(a sin(k.x)), a = -amp*sqrt(rho)*(e1 x k)/|k|^2
+    a = -amp * np.sqrt(rho0) * np.cross(e1, kv) / np.dot(kv, kv)
+    ax = a[0] * np.sin(phase(0.5, 0.0, 0.0))
+    ay = a[1] * np.sin(phase(0.0, 0.5, 0.0))
+    az = a[2] * np.sin(phase(0.0, 0.0, 0.5))
+    b = _edge_potential_curl(ax, ay, az)
+    b += kh[:, None, None, None]
+    e = _energy(rho, m, b, p0)
+    return _pack(rho, m, e, b, dtype)
+
+
+def random_state(nx, ny, nz, seed=0, dtype=np.float32, amp=0.3, bmean=(0.3, 0.1, -0.2)):
+    """Seeded random but physical state (positive density and pressure) used by
+    the per-subroutine parity tests."""
+    r = np.random.default_rng(seed)
+    rho = 1.0 + 0.2 * r.random((nz, ny, nx))
+    m = amp * r.standard_normal((3, nz, ny, nx))
+    b = 0.5 * r.standard_normal((3, nz, ny, nx)) + np.asarray(bmean)[:, None, None, None]
+    p = 1.0 + 0.1 * r.random((nz, ny, nx))
+    e = _energy(rho, m, b, p)
+    return _pack(rho, m, e, b, dtype)
+
+
+def div_b(b, nx, ny, nz):
+    """max |b1(i+1)-b1(i)+b2(j+1)-b2(j)+b3(k+1)-b3(k)| in float64 (left faces)."""
+    bb = np.asarray(b, dtype=np.float64).reshape(nz, ny, nx, 3)
+    d = (np.roll(bb[..., 0], -1, 2) - bb[..., 0] + np.roll(bb[..., 1], -1, 1) - bb[..., 1]
+         + np.roll(bb[..., 2], -1, 0) - bb[..., 2])
+    return float(np.abs(d).max())
+
+
+def totals(u, nx, ny, nz):
+    """FP64 sums of rho, m_x, m_y, m_z, E."""
+    return np.asarray(u, dtype=np.float64).reshape(-1, 5).sum(0)

@@ -1,0 +1,231 @@
+"""Python front end of libmhdgpu.so (ctypes over the C ABI in include/mhdgpu.h).
+
+Device buffers are torch CUDA tensors (flat float32, reference layout); the
+calls are issued on torch's current CUDA stream.  The library is required:
+importing works without it, but every call raises if libmhdgpu.so is missing
+or fails to load.  There is no fallback path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "lib", "libmhdgpu.so")
+
+MHD_OK = 0
+MHD_ERR_ARG = 1
+MHD_ERR_CUDA = 2
+MHD_ERR_TIMEOUT = 3
+MHD_ERR_UNPHYSICAL = 4
+MHD_ERR_NOMEM = 5
+MHD_CFL_C = 0
+MHD_CFL_AVERAGED = 1
+MHD_HEALTH_NONFINITE = 1
+MHD_HEALTH_DENSITY = 2
+MHD_HEALTH_PRESSURE = 4
+KCLASS = {"fluidx": 0, "advectbyzx": 1, "transpose": 2, "cfl": 3}
+
+# every symbol the C headers declare
+EXPORTS = [
+    "mhdgpu_status_string", "mhdgpu_last_error", "mhdgpu_version",
+    "mhdgpu_fluidx", "mhdgpu_advectbyzx_scratch_bytes", "mhdgpu_advectbyzx",
+    "mhdgpu_transpose12", "mhdgpu_transpose13", "mhdgpu_cfl", "mhdgpu_dt_update",
+    "mhdgpu_copy_matrix", "mhdgpu_step_workspace_bytes", "mhdgpu_step", "mhdgpu_advance",
+    "mhdgpu_run_host", "mhdgpu_profiler_create", "mhdgpu_profiler_destroy",
+    "mhdgpu_profiler_attach", "mhdgpu_profiler_reset", "mhdgpu_profiler_summary",
+    # include/mhdgpu_compat.h
+    "fluidx", "advectbyzx", "transpose12", "transpose13", "calcfl", "copy_matrix",
+    "mhdgpu_compat_status",
+]
+
+
+class MhdError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"status {status}: {msg}")
+        self.status = status
+
+
+class Clock(C.Structure):
+    """mhdgpu_clock"""
+    _fields_ = [("t", C.c_float), ("dt", C.c_float), ("inv_c", C.c_float),
+                ("cmax", C.c_uint), ("health", C.c_uint), ("iter", C.c_int)]
+
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"{LIB_PATH} is missing: build it with __graft_entry__.build() "
+                               "or python mhd-gpu_gb300/build.py")
+        L = C.CDLL(LIB_PATH, mode=os.RTLD_LOCAL)
+        P, I, F, D, S = C.c_void_p, C.c_int, C.c_float, C.c_double, C.c_size_t
+        sig = {
+            "mhdgpu_status_string": (C.c_char_p, [I]),
+            "mhdgpu_last_error": (C.c_char_p, []),
+            "mhdgpu_version": (C.c_char_p, []),
+            "mhdgpu_fluidx": (I, [P, P, P, I, I, I, P, P, P]),
+            "mhdgpu_advectbyzx_scratch_bytes": (S, [I, I, I]),
+            "mhdgpu_advectbyzx": (I, [P, P, I, I, I, P, P, P]),
+            "mhdgpu_transpose12": (I, [P, P, P, P, I, I, I, P]),
+            "mhdgpu_transpose13": (I, [P, P, P, P, I, I, I, P]),
+            "mhdgpu_cfl": (I, [P, P, I, I, I, I, P, P, P]),
+            "mhdgpu_dt_update": (I, [P, D, F, P, P, P]),
+            "mhdgpu_copy_matrix": (I, [P, P, P, P, I, I, I, P]),
+            "mhdgpu_step_workspace_bytes": (S, [I, I, I]),
+            "mhdgpu_step": (I, [P, P, I, I, I, P, P, P, P]),
+            "mhdgpu_advance": (I, [P, P, I, I, I, I, D, I, F, P, P, P, P]),
+            "mhdgpu_run_host": (I, [P, P, I, I, I, D, I, P, F, I, P, P]),
+            "mhdgpu_profiler_create": (I, [P, I]),
+            "mhdgpu_profiler_destroy": (I, [P]),
+            "mhdgpu_profiler_attach": (I, [P]),
+            "mhdgpu_profiler_reset": (I, [P]),
+            "mhdgpu_profiler_summary": (I, [P, I, P, P, P]),
+            "calcfl": (F, [P, P, P, P, P]),
+            "mhdgpu_compat_status": (I, []),
+        }
+        for name, (res, args) in sig.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _check(status: int):
+    if status != MHD_OK:
+        raise MhdError(status, lib().mhdgpu_last_error().decode())
+
+
+def _p(t):
+    return None if t is None else C.c_void_p(t.data_ptr())
+
+
+def _stream(stream=None):
+    import torch
+    s = torch.cuda.current_stream() if stream is None else stream
+    return C.c_void_p(s.cuda_stream)
+
+
+def fluidx(u_out, u_in, b, nx, ny, nz, d_dt, health=None, stream=None):
+    _check(lib().mhdgpu_fluidx(_p(u_out), _p(u_in), _p(b), nx, ny, nz, _p(d_dt), _p(health),
+                               _stream(stream)))
+
+
+def advectbyzx_scratch_bytes(nx, ny, nz) -> int:
+    return int(lib().mhdgpu_advectbyzx_scratch_bytes(nx, ny, nz))
+
+
+def advectbyzx(b, u, nx, ny, nz, d_dt, scratch, stream=None):
+    _check(lib().mhdgpu_advectbyzx(_p(b), _p(u), nx, ny, nz, _p(d_dt), _p(scratch), _stream(stream)))
+
+
+def transpose12(dst_u, dst_b, src_u, src_b, nx, ny, nz, stream=None):
+    _check(lib().mhdgpu_transpose12(_p(dst_u), _p(dst_b), _p(src_u), _p(src_b), nx, ny, nz,
+                                    _stream(stream)))
+
+
+def transpose13(dst_u, dst_b, src_u, src_b, nx, ny, nz, stream=None):
+    _check(lib().mhdgpu_transpose13(_p(dst_u), _p(dst_b), _p(src_u), _p(src_b), nx, ny, nz,
+                                    _stream(stream)))
+
+
+def cfl(u, b, nx, ny, nz, mode, d_inv_c, d_word, stream=None):
+    _check(lib().mhdgpu_cfl(_p(u), _p(b), nx, ny, nz, mode, _p(d_inv_c), _p(d_word), _stream(stream)))
+
+
+def dt_update(d_inv_c, cfl_number, tf, d_t, d_dt, stream=None):
+    _check(lib().mhdgpu_dt_update(_p(d_inv_c), float(cfl_number), float(tf), _p(d_t), _p(d_dt),
+                                  _stream(stream)))
+
+
+def step_workspace_bytes(nx, ny, nz) -> int:
+    return int(lib().mhdgpu_step_workspace_bytes(nx, ny, nz))
+
+
+def step(u, b, nx, ny, nz, d_dt, work, health=None, stream=None):
+    _check(lib().mhdgpu_step(_p(u), _p(b), nx, ny, nz, _p(d_dt), _p(work), _p(health),
+                             _stream(stream)))
+
+
+def advance(u, b, nx, ny, nz, nsteps, cfl_number, cfl_mode, tf, clock, dt_log, work, stream=None):
+    """clock: a torch uint8 CUDA tensor of sizeof(Clock) bytes (see new_clock)."""
+    _check(lib().mhdgpu_advance(_p(u), _p(b), nx, ny, nz, int(nsteps), float(cfl_number),
+                                int(cfl_mode), float(tf), _p(clock), _p(dt_log), _p(work),
+                                _stream(stream)))
+
+
+def new_clock(device="cuda", t=0.0):
+    import torch
+    host = Clock()
+    host.t = t
+    raw = bytes(host)
+    return torch.tensor(list(raw), dtype=torch.uint8, device=device)
+
+
+def read_clock(clock) -> Clock:
+    data = bytes(clock.cpu().numpy().tobytes())
+    return Clock.from_buffer_copy(data)
+
+
+def run_host(u, b, nx, ny, nz, cfl_number=0.9, cfl_mode=MHD_CFL_C, t=0.0, tf=0.0,
+             max_steps=1, dt_log=None):
+    """End-to-end call on host numpy arrays (float32, modified in place).
+
+    Returns (status, t, steps_done); status MHD_ERR_UNPHYSICAL is returned, not
+    raised, so that the caller can inspect the state."""
+    import numpy as np
+    assert u.dtype == np.float32 and b.dtype == np.float32
+    tt = C.c_float(t)
+    done = C.c_int(0)
+    log_ptr = None if dt_log is None else dt_log.ctypes.data_as(C.c_void_p)
+    st = lib().mhdgpu_run_host(u.ctypes.data_as(C.c_void_p), b.ctypes.data_as(C.c_void_p), nx, ny,
+                               nz, float(cfl_number), int(cfl_mode), C.byref(tt), float(tf),
+                               int(max_steps), log_ptr, C.byref(done))
+    if st not in (MHD_OK, MHD_ERR_UNPHYSICAL):
+        _check(st)
+    return st, tt.value, done.value
+
+
+class Profiler:
+    """Per-kernel-class device time from CUDA events (mhdgpu_profiler_*).
+
+    Use as a context manager around the C-ABI calls to time; ``summary()``
+    returns {class: (records, launches, total_ms)}."""
+
+    def __init__(self, max_records=100000):
+        self.h = C.c_void_p()
+        _check(lib().mhdgpu_profiler_create(C.byref(self.h), int(max_records)))
+
+    def __enter__(self):
+        _check(lib().mhdgpu_profiler_attach(self.h))
+        return self
+
+    def __exit__(self, *exc):
+        lib().mhdgpu_profiler_attach(None)
+        return False
+
+    def reset(self):
+        _check(lib().mhdgpu_profiler_reset(self.h))
+
+    def summary(self):
+        out = {}
+        for name, k in KCLASS.items():
+            r, n, ms = C.c_int(), C.c_int(), C.c_double()
+            _check(lib().mhdgpu_profiler_summary(self.h, k, C.byref(r), C.byref(n), C.byref(ms)))
+            out[name] = (r.value, n.value, ms.value)
+        return out
+
+    def close(self):
+        if self.h:
+            lib().mhdgpu_profiler_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,84 @@
+"""CPU tests of the C ABI: the library builds and loads, exports every symbol
+the headers declare, and rejects bad arguments before touching the GPU."""
+import ctypes as C
+import os
+import re
+
+import pytest
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _declared_functions():
+    names = []
+    for h in ("mhdgpu.h", "mhdgpu_compat.h"):
+        src = open(os.path.join(REPO, "include", h)).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        for m in re.finditer(r"^\s*[A-Za-z_][\w\s\*]*?\b([A-Za-z_]\w*)\s*\(", src, flags=re.M):
+            name = m.group(1)
+            if name not in ("defined",) and not name.isupper():
+                names.append(name)
+    return sorted(set(names))
+
+
+@pytest.fixture(scope="module")
+def L():
+    import mhdgpu
+    if not os.path.exists(mhdgpu.LIB_PATH):
+        import build
+        build.build()
+    return mhdgpu.lib()
+
+
+def test_headers_declare_the_python_export_list():
+    import mhdgpu
+    assert set(_declared_functions()) == set(mhdgpu.EXPORTS)
+
+
+def test_library_exports_every_declared_symbol(L):
+    for name in _declared_functions():
+        assert hasattr(L, name), name
+
+
+def test_status_strings(L):
+    assert L.mhdgpu_status_string(0) == b"ok"
+    assert L.mhdgpu_status_string(1) == b"invalid argument"
+    assert b"sm_103a" in L.mhdgpu_version()
+
+
+def test_bad_arguments_are_rejected_without_a_gpu(L):
+    import mhdgpu
+    P = C.c_void_p
+    fake = P(0x1000)
+    # zero-size box
+    assert L.mhdgpu_fluidx(fake, fake, fake, 0, 4, 4, fake, None, None) == mhdgpu.MHD_ERR_ARG
+    assert b"bad box" in L.mhdgpu_last_error()
+    # pencil longer than the kernels accept
+    assert L.mhdgpu_fluidx(fake, fake, fake, 4096, 1, 1, fake, None, None) == mhdgpu.MHD_ERR_ARG
+    # null pointers
+    assert L.mhdgpu_fluidx(None, fake, fake, 8, 8, 8, fake, None, None) == mhdgpu.MHD_ERR_ARG
+    assert L.mhdgpu_advectbyzx(fake, fake, 8, 8, 8, fake, None, None) == mhdgpu.MHD_ERR_ARG
+    # transposes must be out of place
+    assert L.mhdgpu_transpose12(fake, fake, fake, fake, 8, 8, 8, None) == mhdgpu.MHD_ERR_ARG
+    assert b"out of place" in L.mhdgpu_last_error()
+    # bad CFL mode
+    assert L.mhdgpu_cfl(fake, fake, 8, 8, 8, 7, fake, fake, None) == mhdgpu.MHD_ERR_ARG
+    # negative step count, bad cfl number
+    assert L.mhdgpu_advance(fake, fake, 8, 8, 8, -1, 0.9, 0, 0.0, fake, None, fake, None) == mhdgpu.MHD_ERR_ARG
+    assert L.mhdgpu_advance(fake, fake, 8, 8, 8, 1, 0.0, 0, 0.0, fake, None, fake, None) == mhdgpu.MHD_ERR_ARG
+    assert L.mhdgpu_dt_update(fake, -1.0, 0.0, fake, fake, None) == mhdgpu.MHD_ERR_ARG
+
+
+def test_partial_overlap_rejected(L):
+    import mhdgpu
+    base = 0x100000
+    n5 = 5 * 8 * 8 * 8 * 4
+    st = L.mhdgpu_fluidx(C.c_void_p(base + 4), C.c_void_p(base), C.c_void_p(base + 10 * n5), 8, 8, 8,
+                         C.c_void_p(base), None, None)
+    assert st == mhdgpu.MHD_ERR_ARG
+
+
+def test_workspace_sizes(L):
+    assert L.mhdgpu_step_workspace_bytes(32, 32, 32) == 40 * 32 ** 3
+    assert L.mhdgpu_advectbyzx_scratch_bytes(16, 8, 4) == 8 * 16 * 8 * 4
+    assert L.mhdgpu_step_workspace_bytes(0, 1, 1) == 0

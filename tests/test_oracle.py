@@ -1,0 +1,139 @@
+"""CPU tests of the oracle: pinned to the reference's own C path through the
+golden vectors (which the reference produced, tests/golden/gen_golden.py)
+and, where the reference has been compiled here (oracle/_ref), directly."""
+import os
+
+import numpy as np
+import pytest
+
+from util import bits_equal, field_errors
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def test_oracle_matches_reference_goldens_per_subroutine(oracle_lib):
+    O = oracle_lib.oracle("f32")
+    g = np.load(os.path.join(GOLD, "subroutines_f32.npz"))
+    tags = sorted({k.split("_")[0] for k in g.files})
+    assert tags
+    for tag in tags:
+        nx, ny, nz = (int(x) for x in g[f"{tag}_dims"])
+        dt = np.float32(g[f"{tag}_dt"][0])
+        u, b = g[f"{tag}_u"], g[f"{tag}_b"]
+        uu = np.zeros_like(u)
+        O.fluidx(uu, b.copy(), nx, ny, nz, dt, u.copy(), b.copy())
+        assert bits_equal(uu, g[f"{tag}_fluidx_u"]), tag
+        bb = b.copy()
+        O.advectbyzx(u.copy(), bb, nx, ny, nz, dt, u.copy(), b.copy())
+        assert bits_equal(bb, g[f"{tag}_advect_b"]), tag
+        tu, tb = np.zeros_like(u), np.zeros_like(b)
+        O.transpose12(tu, tb, u.copy(), b.copy(), nx, ny, nz)
+        assert bits_equal(tu, g[f"{tag}_t12_u"]) and bits_equal(tb, g[f"{tag}_t12_b"]), tag
+        if f"{tag}_t13_u" in g.files:
+            tu, tb = np.zeros_like(u), np.zeros_like(b)
+            O.transpose13(tu, tb, u.copy(), b.copy(), nx, ny, nz)
+            assert bits_equal(tu, g[f"{tag}_t13_u"]) and bits_equal(tb, g[f"{tag}_t13_b"]), tag
+        assert bits_equal(np.array([O.calcfl(u, b, nx, ny, nz)]), g[f"{tag}_calcfl"]), tag
+
+
+def test_oracle_matches_reference_run_on_shipped_alfven_state(oracle_lib):
+    """54 steps to tf=64 from data/source_init_alfvenlinear_16cube.dat, CFL 0.9:
+    the reference's own run (Heterogeneous_MHD/C/mhd.c:59-125), bit for bit."""
+    O = oracle_lib.oracle("f32")
+    g = np.load(os.path.join(GOLD, "alfven16_dat.npz"))
+    u, b = g["u0"].copy(), g["b0"].copy()
+    s, t, dts = O.run(u, b, 16, 16, 16, cfl_number=0.9, tf=64.0, max_steps=100000)
+    assert s == int(g["steps"][0]) == 54
+    assert bits_equal(dts, g["dtsf"])
+    assert np.float32(t) == g["t"][0]
+    assert bits_equal(u, g["uf"]) and bits_equal(b, g["bf"])
+
+
+def test_oracle_matches_reference_cfl07_alfven_x(oracle_lib):
+    O = oracle_lib.oracle("f32")
+    g = np.load(os.path.join(GOLD, "alfvenx16_cfl07.npz"))
+    u, b = g["u0"].copy(), g["b0"].copy()
+    s, t, dts = O.run(u, b, 16, 16, 16, cfl_number=0.7, tf=0.0, max_steps=20)
+    assert s == 20 and bits_equal(dts, g["dts"])
+    assert bits_equal(u, g["u"]) and bits_equal(b, g["b"])
+
+
+def test_oracle64_matches_reference_fp64_build(oracle_lib):
+    O = oracle_lib.oracle("f64")
+    g = np.load(os.path.join(GOLD, "run8_f64.npz"))
+    u, b = g["u0"].copy(), g["b0"].copy()
+    s, t, dts = O.run(u, b, 8, 8, 8, cfl_number=0.9, tf=0.0, max_steps=3)
+    assert bits_equal(dts, g["dts"])
+    assert bits_equal(u, g["u"]) and bits_equal(b, g["b"])
+
+
+def test_oracle_thread_count_invariant(oracle_lib):
+    import ics
+    O = oracle_lib.oracle("f32")
+    u0, b0 = ics.random_state(12, 10, 8, seed=3)
+    res = []
+    for th in (1, 4):
+        oracle_lib.set_threads(th)
+        u, b = u0.copy(), b0.copy()
+        O.run(u, b, 12, 10, 8, cfl_number=0.8, max_steps=2)
+        res.append((u, b))
+    oracle_lib.set_threads(1)
+    assert bits_equal(res[0][0], res[1][0]) and bits_equal(res[0][1], res[1][1])
+
+
+def test_oracle_fp32_close_to_fp64_on_alfven(oracle_lib):
+    import ics
+    O32, O64 = oracle_lib.oracle("f32"), oracle_lib.oracle("f64")
+    u, b = ics.alfven_x(16)
+    u64, b64 = u.astype(np.float64), b.astype(np.float64)
+    O32.run(u, b, 16, 16, 16, cfl_number=0.7, max_steps=10)
+    O64.run(u64, b64, 16, 16, 16, cfl_number=0.7, max_steps=10)
+    eu, eb = field_errors(u, u64, 5), field_errors(b, b64, 3)
+    # the wave (rho, m_y, E, b_x, b_y) to 1e-5 of each field
+    for e in (eu[0], eu[2], eu[4], eb[0], eb[1]):
+        assert e < 1e-5, (eu, eb)
+    # m_x is second order (~3e-7) and FP32 pressure round-off (~1e-7
+    # absolute) dominates it; bound it against the total pressure scale
+    ux, u64x = u.reshape(-1, 5), u64.reshape(-1, 5)
+    assert np.abs(ux[:, 1] - u64x[:, 1]).max() < 1e-6
+
+
+def test_oracle_transpose13_noncubic_is_the_fortran_formula(oracle_lib):
+    """nx != nz: dst(ii,k,j,i) = src(perm(ii),i,j,k), perm_u=(1,4,3,2,5),
+    perm_b=(3,2,1) (OpenMP/mhd.f90:433-474); applying it twice is the identity."""
+    import ics
+    O = oracle_lib.oracle("f32")
+    nx, ny, nz = 6, 5, 9
+    u, b = ics.random_state(nx, ny, nz, seed=5)
+    tu, tb = np.zeros_like(u), np.zeros_like(b)
+    O.transpose13(tu, tb, u.copy(), b.copy(), nx, ny, nz)
+    U = u.reshape(nz, ny, nx, 5)
+    T = tu.reshape(nx, ny, nz, 5)   # dims (nz, ny, nx) -> index [i][j][k]
+    assert np.array_equal(T, U[..., [0, 3, 2, 1, 4]].transpose(2, 1, 0, 3))
+    bu, bb = np.zeros_like(u), np.zeros_like(b)
+    O.transpose13(bu, bb, tu, tb, nz, ny, nx)
+    assert bits_equal(bu, u) and bits_equal(bb, b)
+
+
+@pytest.mark.skipif(not os.path.exists(os.path.join(os.path.dirname(os.path.dirname(
+    os.path.abspath(__file__))), "oracle", "_ref", "libref_f32.so")),
+    reason="reference C path not compiled here (make -C oracle ref)")
+def test_oracle_bit_exact_against_reference_build(oracle_lib):
+    import ics
+    R, O = oracle_lib.reference("f32"), oracle_lib.oracle("f32")
+    for dims, seed in [((8, 8, 8), 1), ((12, 6, 10), 2), ((5, 7, 9), 3), ((16, 4, 16), 4)]:
+        nx, ny, nz = dims
+        u0, b0 = ics.random_state(*dims, seed=seed)
+        out = []
+        for P in (R, O):
+            u, b = u0.copy(), b0.copy()
+            if nx == ny == nz:
+                P.run(u, b, nx, ny, nz, cfl_number=0.9, max_steps=2)
+            else:
+                uu = np.zeros_like(u)
+                P.fluidx(uu, b.copy(), nx, ny, nz, np.float32(0.05), u.copy(), b.copy())
+                bb = b.copy()
+                P.advectbyzx(u.copy(), bb, nx, ny, nz, np.float32(0.05), u.copy(), b.copy())
+                u, b = uu, bb
+            out.append((u, b))
+        assert bits_equal(out[0][0], out[1][0]) and bits_equal(out[0][1], out[1][1]), dims
