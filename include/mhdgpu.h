@@ -37,7 +37,7 @@ typedef struct CUstream_st *mhdgpu_stream_t;
 #define MHD_ERR_ARG         1   /* bad size, null pointer, aliasing, unsupported shape */
 #define MHD_ERR_CUDA        2   /* a CUDA runtime call failed */
 #define MHD_ERR_TIMEOUT     3   /* a bounded device wait gave up */
-#define MHD_ERR_UNPHYSICAL  4   /* the health word reports NaN/Inf, rho<=0 or p<=0 */
+#define MHD_ERR_UNPHYSICAL  4   /* the health word reports NaN/Inf or rho<=0 */
 #define MHD_ERR_NOMEM       5   /* a host-buffer entry could not allocate */
 
 /* CFL formulas */
@@ -49,7 +49,12 @@ typedef struct CUstream_st *mhdgpu_stream_t;
 /* device health word bits (OR-ed by the kernels, read by the host) */
 #define MHD_HEALTH_NONFINITE 1u  /* NaN or Inf in an updated state */
 #define MHD_HEALTH_DENSITY   2u  /* rho <= 0 */
-#define MHD_HEALTH_PRESSURE  4u  /* gas pressure <= 0 at the RK2 full step */
+#define MHD_HEALTH_PRESSURE  4u  /* gas pressure <= 0 at the RK2 full step: a warning.
+                                    In FP32 the recovery p = ps - B^2/2 cancels at low
+                                    plasma beta and dips below 0 at round-off; the
+                                    reference solver runs through it (it takes |.| in
+                                    the fast speed, C/mhdflux.c:45), and so does this
+                                    one.  Only NONFINITE and DENSITY fail a run. */
 
 /* largest pencil the device kernels accept (cells along the frame's x) */
 #define MHD_MAX_PENCIL      1024

@@ -285,7 +285,8 @@ int mhdgpu_run_host(float *u, float *b, int nx, int ny, int nz, double cfl_numbe
             RH(cudaMemcpy(dt_log, dlog, sizeof(float) * h.iter, cudaMemcpyDeviceToHost), "mhdgpu_run_host: dt log");
         *t = h.t;
         if (steps_done) *steps_done = h.iter;
-        if (h.health) ret = fail(MHD_ERR_UNPHYSICAL, "mhdgpu_run_host: health word set (NaN/Inf, rho<=0 or p<=0)");
+        if (h.health & (MHD_HEALTH_NONFINITE | MHD_HEALTH_DENSITY))
+            ret = fail(MHD_ERR_UNPHYSICAL, "mhdgpu_run_host: health word reports NaN/Inf or rho <= 0");
     }
 done:
     if (s) {

@@ -66,7 +66,7 @@ transpose_kernel(TransposeArgs t)
         const int bb = col / 5, cc = col - bb * 5;
         if (s < na && bb < nb) {
             const long long cell = (long long)b0 + (long long)(a0 + s) * t.sa_out + o * t.so_out;
-            t.du[cell * 5 + cc] = tu[bb * kRowU + s * 5 + ((t.pu >> (4 * cc)) & 15u)];
+            t.du[cell * 5 + col] = tu[bb * kRowU + s * 5 + ((t.pu >> (4 * cc)) & 15u)];
         }
     }
     for (int e = threadIdx.x; e < kTile * kTile * 3; e += blockDim.x) {
@@ -74,7 +74,7 @@ transpose_kernel(TransposeArgs t)
         const int bb = col / 3, cc = col - bb * 3;
         if (s < na && bb < nb) {
             const long long cell = (long long)b0 + (long long)(a0 + s) * t.sa_out + o * t.so_out;
-            t.db[cell * 3 + cc] = tb[bb * kRowB + s * 3 + ((t.pb >> (4 * cc)) & 15u)];
+            t.db[cell * 3 + col] = tb[bb * kRowB + s * 3 + ((t.pb >> (4 * cc)) & 15u)];
         }
     }
 }
