@@ -87,6 +87,23 @@ size_t mhdgpu_advectbyzx_scratch_bytes(int nx, int ny, int nz);
 int mhdgpu_advectbyzx(float *b, const float *u, int nx, int ny, int nz,
                       const float *d_dt, float *d_scratch, mhdgpu_stream_t stream);
 
+/* advectbyzx for callers that cannot allocate device memory.  No counterpart
+ * in the reference (whose CUDA wrapper takes caller scratch, d_temp).
+ * Same result as mhdgpu_advectbyzx, but the two floats of scratch per cell
+ * come from a fixed array inside the library (MHD_NOALLOC_MAX_CELLS * 8
+ * bytes = 16 MiB, held on every GPU that loads the library until exit), so a
+ * caller that owns only its inputs and outputs -- a plugin running inside
+ * another runtime's memory pool, or a loop that must not allocate -- can run
+ * it.  It allocates nothing.  Boxes above MHD_NOALLOC_MAX_CELLS cells are
+ * rejected with MHD_ERR_ARG.  The first call on a device looks up the array's
+ * device address with that device current; make it before any stream
+ * capture.  All calls share the array, so calls that overlap on the GPU race
+ * and must be serialised by the caller.  Nothing in the array has to start at
+ * zero: each call writes every entry it reads. */
+#define MHD_NOALLOC_MAX_CELLS 2097152   /* 128^3 */
+int mhdgpu_advectbyzx_noalloc(float *b, const float *u, int nx, int ny, int nz,
+                              const float *d_dt, mhdgpu_stream_t stream);
+
 /* transpose12: (nx,ny,nz) -> (ny,nx,nz), u components (1,3,2,4,5) and b
  * components (2,1,3) (1-based).  Out of place; bit-exact.
  * Replaces Cuda/cuda_transpose12.cu:12-38 and C/transpose12.c:7-47. */

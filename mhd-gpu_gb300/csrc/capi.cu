@@ -19,6 +19,11 @@ using namespace mhd;
 
 static thread_local char g_err[512];
 
+void mhd::set_last_error(const char *msg)
+{
+    snprintf(g_err, sizeof g_err, "%s", msg);
+}
+
 static int fail(int status, const char *fmt, const char *detail = nullptr)
 {
     if (detail) snprintf(g_err, sizeof g_err, fmt, detail);

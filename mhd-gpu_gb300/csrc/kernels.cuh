@@ -44,4 +44,7 @@ cudaError_t launch_dt_update(const float *inv_c, double cfl_number, float tf, fl
 cudaError_t launch_clock(mhdgpu_clock *clk, double cfl_number, float tf, float *dt_log,
                          cudaStream_t s);
 
+// sets the calling thread's message returned by mhdgpu_last_error()
+void set_last_error(const char *msg);
+
 }  // namespace mhd

@@ -30,6 +30,7 @@ KCLASS = {"fluidx": 0, "advectbyzx": 1, "transpose": 2, "cfl": 3}
 EXPORTS = [
     "mhdgpu_status_string", "mhdgpu_last_error", "mhdgpu_version",
     "mhdgpu_fluidx", "mhdgpu_advectbyzx_scratch_bytes", "mhdgpu_advectbyzx",
+    "mhdgpu_advectbyzx_noalloc",
     "mhdgpu_transpose12", "mhdgpu_transpose13", "mhdgpu_cfl", "mhdgpu_dt_update",
     "mhdgpu_copy_matrix", "mhdgpu_step_workspace_bytes", "mhdgpu_step", "mhdgpu_advance",
     "mhdgpu_run_host", "mhdgpu_profiler_create", "mhdgpu_profiler_destroy",
@@ -70,6 +71,7 @@ def lib() -> C.CDLL:
             "mhdgpu_fluidx": (I, [P, P, P, I, I, I, P, P, P]),
             "mhdgpu_advectbyzx_scratch_bytes": (S, [I, I, I]),
             "mhdgpu_advectbyzx": (I, [P, P, I, I, I, P, P, P]),
+            "mhdgpu_advectbyzx_noalloc": (I, [P, P, I, I, I, P, P]),
             "mhdgpu_transpose12": (I, [P, P, P, P, I, I, I, P]),
             "mhdgpu_transpose13": (I, [P, P, P, P, I, I, I, P]),
             "mhdgpu_cfl": (I, [P, P, I, I, I, I, P, P, P]),
