@@ -66,7 +66,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
-                 "--format=csv,noheader,nounits", "-lms", "100"],
+                 "--format=csv,noheader,nounits", "-lms", "25"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except OSError:
             self.proc = None
@@ -199,6 +199,8 @@ def main():
     ap.add_argument("--n", type=int, default=128)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--math", default="faithful", choices=["faithful", "fast"])
+    ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (default tiles)")
     args = ap.parse_args()
     n, K, W = args.n, args.steps, max(3, args.warmup)
     ncell = n ** 3
@@ -237,59 +239,74 @@ def main():
 
     rank, world, local = dist_setup(args.gpus)
     dev = torch.device("cuda", local if world > 1 else 0)
+    math_mode = mhdgpu.MHD_MATH_FAST if args.math == "fast" else mhdgpu.MHD_MATH_FAITHFUL
+    mhdgpu.set_math(math_mode)
+    if not args.no_tune:
+        picks = mhdgpu.autotune(n, n, n, math_mode)
+    else:
+        picks = {(k, n, r): mhdgpu.get_tile(k, n, rows=r) for k in ("fluidx", "advectbyzx")
+                 for r in (False, True)}
+    config["math"] = args.math
+    config["tiles"] = {f"{k}@{m}{'/rows' if r else ''}": list(v) for (k, m, r), v in picks.items()}
+    config["tiles_from"] = "defaults" if args.no_tune else "mhdgpu_autotune"
     u0, b0 = ics.alfven_oblique(n)
-    du = torch.from_numpy(u0).to(dev)
-    db = torch.from_numpy(b0).to(dev)
-    work = torch.empty(mhdgpu.step_workspace_bytes(n, n, n), dtype=torch.uint8, device=dev)
-    clock = mhdgpu.new_clock(device=dev)
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
     stream = torch.cuda.Stream(device=dev)
-
-    def one_step():
-        mhdgpu.advance(du, db, n, n, n, 1, 0.7, mhdgpu.MHD_CFL_C, 0.0, clock, None, work)
-
-    # warm-up (also sets kernel attributes before capture)
-    with torch.cuda.stream(stream):
-        for _ in range(W):
-            one_step()
-    torch.cuda.synchronize()
-    graph = torch.cuda.CUDAGraph()
-    with torch.cuda.graph(graph, stream=stream):
-        one_step()
-    torch.cuda.synchronize()
-
     vis = [x.strip() for x in os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",") if x.strip()]
     sampler = ClockSampler(vis[local] if len(vis) > local else local)
     sampler.start()
     time.sleep(0.3)
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
-    dist_barrier(world)
-    torch.cuda.synchronize()
-    t_wall0 = time.time()
-    with torch.cuda.stream(stream):
-        for i in range(K):
-            flush.zero_()
-            ev[i][0].record(stream)
-            graph.replay()
-            ev[i][1].record(stream)
-    torch.cuda.synchronize()
-    t_wall1 = time.time()
-    dist_barrier(world)
-    step_ms = [a.elapsed_time(b) for a, b in ev]
-    total_s = dist_max(sum(step_ms) / 1e3, world)
-    value = world * ncell * K / total_s
 
-    # profiled pass: same steps launched directly, CUDA events around every
-    # kernel class (per-launch device time of the dominant kernel)
-    prof = mhdgpu.Profiler(max_records=K * 40 + 100)
-    with torch.cuda.stream(stream):
-        with prof:
+    def measure(path):
+        """K graph-replayed steps (L2 flushed between them, outside the
+        events), then K directly launched steps under the event profiler."""
+        du = torch.from_numpy(u0).to(dev)
+        db = torch.from_numpy(b0).to(dev)
+        work = torch.empty(mhdgpu.step_workspace_bytes(n, n, n, path), dtype=torch.uint8, device=dev)
+        clock = mhdgpu.new_clock(device=dev)
+
+        def one_step():
+            mhdgpu.advance(du, db, n, n, n, 1, 0.7, mhdgpu.MHD_CFL_C, 0.0, clock, None, work, path)
+
+        with torch.cuda.stream(stream):          # warm-up; sets kernel attributes before capture
+            for _ in range(W):
+                one_step()
+        torch.cuda.synchronize()
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph, stream=stream):
+            one_step()
+        torch.cuda.synchronize()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
+        dist_barrier(world)
+        torch.cuda.synchronize()
+        tw0 = time.time()
+        with torch.cuda.stream(stream):
             for i in range(K):
                 flush.zero_()
-                one_step()
-    torch.cuda.synchronize()
-    summ = prof.summary()
-    prof.close()
+                ev[i][0].record(stream)
+                graph.replay()
+                ev[i][1].record(stream)
+        torch.cuda.synchronize()
+        tw1 = time.time()
+        dist_barrier(world)
+        total_s = dist_max(sum(a.elapsed_time(b) for a, b in ev) / 1e3, world)
+        prof = mhdgpu.Profiler(max_records=K * 40 + 100)
+        with torch.cuda.stream(stream):
+            with prof:
+                for i in range(K):
+                    flush.zero_()
+                    one_step()
+        torch.cuda.synchronize()
+        summ = prof.summary()
+        prof.close()
+        health = mhdgpu.read_clock(clock).health
+        del graph
+        return total_s, summ, health, (tw0, tw1)
+
+    total_s, summ, health, (t_wall0, t_wall1) = measure(mhdgpu.MHD_PATH_FUSED)
+    value = world * ncell * K / total_s
+    plain_s, plain_summ, plain_health, _ = measure(mhdgpu.MHD_PATH_PLAIN)
+    value_plain = world * ncell * K / plain_s
     sampler.stop()
     clocks = sampler.summary(t_wall0, t_wall1)
     launches_per_step = sum(v[1] for v in summ.values()) / K
@@ -307,15 +324,15 @@ def main():
     un, bn = hu.numpy(), hb.numpy()
     ke = max(3, min(K, 50))
     t = 0.0
-    mhdgpu.run_host(un, bn, n, n, n, 0.7, 0, t, 0.0, 1)
+    mhdgpu.run_host(un, bn, n, n, n, 0.7, 0, t, 0.0, 1, path=mhdgpu.MHD_PATH_FUSED)
     dist_barrier(world)
     t0 = time.perf_counter()
     for _ in range(ke):
-        st, t, _done = mhdgpu.run_host(un, bn, n, n, n, 0.7, 0, t, 0.0, 1)
+        st, t, _done = mhdgpu.run_host(un, bn, n, n, n, 0.7, 0, t, 0.0, 1, path=mhdgpu.MHD_PATH_FUSED)
     e2e_s = dist_max(time.perf_counter() - t0, world)
     e2e = world * ncell * ke / e2e_s
+    config["path"] = "transpose-free step (mhdgpu_step_fused), one CUDA graph per step"
 
-    health = mhdgpu.read_clock(clock).health
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
         "ms_per_step": total_s / K * 1e3, "higher_is_better": True, "scaling": "weak",
@@ -323,7 +340,10 @@ def main():
         "data": "synthetic (seedless analytic initial state, see config.ic)",
         "config": config,
         "gpu_launches": int(round(launches_per_step * K)),
-        "roofline": {"bound": "hbm", "kernel": "fluidx_kernel<4,1>",
+        "roofline": {"bound": "hbm",
+                     "kernel": "fluidx_kernel (x sweep %s, y/z sweeps %s [cpl,wpp,ppc], %s)" % (
+                         list(mhdgpu.get_tile("fluidx", n)), list(mhdgpu.get_tile("fluidx", n, rows=True)),
+                         args.math),
                      "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
                      "traffic": traffic,
@@ -336,6 +356,11 @@ def main():
                           "frac_plain_pass_bytes": value * PLAIN_PASS_BYTES / 1e9 / world / hbm},
         "kernel_time_ms_per_step": {k: v[2] / K for k, v in summ.items()},
         "kernel_launches_per_step": {k: v[1] / K for k, v in summ.items()},
+        "plain_drop_in": {"value": value_plain, "unit": UNIT, "ms_per_step": plain_s / K * 1e3,
+                          "path": "per-subroutine kernels + transposes (mhdgpu_step)",
+                          "kernel_time_ms_per_step": {k: v[2] / K for k, v in plain_summ.items()},
+                          "health": plain_health},
+        "fused_over_plain": value / value_plain,
         "e2e": {"value": e2e, "unit": UNIT, "steps": ke,
                 "h2d_bytes_per_step": 32 * ncell, "d2h_bytes_per_step": 32 * ncell,
                 "api": "mhdgpu_run_host, 1 step per call"},

@@ -148,6 +148,19 @@ size_t mhdgpu_step_workspace_bytes(int nx, int ny, int nz);
 int mhdgpu_step(float *u, float *b, int nx, int ny, int nz, const float *d_dt,
                 void *d_work, unsigned *d_health, mhdgpu_stream_t stream);
 
+/* The same step without transposes: the y and z sweeps read and write their
+ * pencils in place in the x-major state through strided views (the frames of
+ * C/mhd.c:79-113 after transpose12/13), so no data moves between sweeps.  Each
+ * sweep is a fluid kernel, a field-advection kernel and a b(1) gather; the
+ * arithmetic per pencil is that of mhdgpu_step, bit for bit.  Workspace:
+ * mhdgpu_step_fused_workspace_bytes (8 bytes per cell). */
+size_t mhdgpu_step_fused_workspace_bytes(int nx, int ny, int nz);
+int mhdgpu_step_fused(float *u, float *b, int nx, int ny, int nz, const float *d_dt,
+                      void *d_work, unsigned *d_health, mhdgpu_stream_t stream);
+
+#define MHD_PATH_PLAIN      0   /* mhdgpu_step: per-subroutine kernels + transposes */
+#define MHD_PATH_FUSED      1   /* mhdgpu_step_fused: transpose-free */
+
 /* clock of a run kept on the device */
 typedef struct {
     float t;        /* simulation time */
@@ -160,22 +173,55 @@ typedef struct {
 
 /* nsteps iterations of: CFL -> dt update -> step, all on the device
  * (C/mhd.c:60-125 without its printfs).  d_dt_log (may be NULL) receives each
- * step's dt at d_dt_log[clock.iter].  Steps with tf > 0 and t >= tf are
- * skipped on the device (the reference's do-while exit). */
+ * step's dt at d_dt_log[clock.iter], so it must hold clock.iter + nsteps
+ * entries.  Steps with tf > 0 and t >= tf are skipped on the device (the
+ * reference's do-while exit).  path = MHD_PATH_PLAIN (d_work of
+ * mhdgpu_step_workspace_bytes) or MHD_PATH_FUSED (of
+ * mhdgpu_step_fused_workspace_bytes). */
 int mhdgpu_advance(float *u, float *b, int nx, int ny, int nz, int nsteps,
                    double cfl_number, int cfl_mode, float tf,
                    mhdgpu_clock *d_clock, float *d_dt_log, void *d_work,
-                   mhdgpu_stream_t stream);
+                   int path, mhdgpu_stream_t stream);
 
 /* ------------------------------------------------------------------------
  * Host-buffer entry (the end-to-end path): uploads (u, b) from host memory,
  * runs up to max_steps steps as mhdgpu_advance does, downloads the state.
  * Allocates its device buffers per call.  *t is read and updated; dt_log may
- * be NULL.  Returns the steps taken in *steps_done (may be NULL).
+ * be NULL.  Returns the steps taken in *steps_done (may be NULL).  path as
+ * for mhdgpu_advance.
  * ------------------------------------------------------------------------ */
 int mhdgpu_run_host(float *u, float *b, int nx, int ny, int nz, double cfl_number,
                     int cfl_mode, float *t, float tf, int max_steps, float *dt_log,
-                    int *steps_done);
+                    int *steps_done, int path);
+
+/* ------------------------------------------------------------------------
+ * Arithmetic policy and tile shapes (process-wide settings, host side).
+ * ------------------------------------------------------------------------ */
+#define MHD_MATH_FAITHFUL   0   /* rounding of the reference C path (default) */
+#define MHD_MATH_FAST       1   /* plain FP32 with FMA contraction, hardware
+                                   reciprocal and root: faster, ~1 ulp per op
+                                   further from the reference */
+
+/* selects the policy of the fluid kernels; returns the previous one */
+int mhdgpu_set_math(int mode);
+
+/* Team shape of a pencil kernel (kclass MHD_KCLASS_FLUIDX or
+ * MHD_KCLASS_ADVECT, OR-ed with MHD_TILE_ROWS for pencils that run across
+ * memory -- the y and z sweeps of mhdgpu_step_fused) for pencils of length n:
+ * cpl cells per thread, wpp warps per pencil, ppc pencils per CTA;
+ * n <= 32*wpp*cpl and 32*wpp*ppc <= 256.  mhdgpu_set_tile overrides the
+ * default table; mhdgpu_get_tile reports the shape in use.  Compiled shapes
+ * (cpl,wpp): (1,1) (2,1) (4,1) (1,2) (2,2) (4,2) (1,4) (2,4) (4,4) (2,8) (4,8). */
+#define MHD_TILE_ROWS       16
+int mhdgpu_set_tile(int kclass, int n, int cpl, int wpp, int ppc);
+int mhdgpu_get_tile(int kclass, int n, int *cpl, int *wpp, int *ppc);
+
+/* Autotuner: for each pencil length the step uses on an nx*ny*nz box (nx, ny
+ * and nz), times every compiled shape of the fluid and advection kernels on a
+ * synthetic state of this box with CUDA events, keeps the fastest through
+ * mhdgpu_set_tile and returns.  Allocates and frees its own test buffers;
+ * synchronises the device.  Not for use under stream capture. */
+int mhdgpu_autotune(int nx, int ny, int nz, int math);
 
 /* ------------------------------------------------------------------------
  * Profiler: per-kernel-class device time from CUDA events.  While a profiler

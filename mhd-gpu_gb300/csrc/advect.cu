@@ -1,117 +1,195 @@
 // advect.cu - constrained-transport advection of the transverse face fields
-// (advectbyzx) on pencils of the reference layout, for sm_103a.
+// (advectbyzx) on pencils of a frame view, for sm_103a.
 //
 // Algorithm: Heterogeneous_MHD/C/advectbyzx.c:14-23 with advectbyzxA1.c:18-63,
 // A2.c:9-28, B1.c:19-62, B2.c:9-29 and the upwind/van Leer 1-D update tvdb.c:10-91.
 //
-// The reference scatters b_x(j-1) += flux(j) through a full-grid temporary in
+// The reference scatters b(1)(j-1) += flux(j) through a full-grid temporary in
 // a second pass.  Here:
-//   kernel 1 (per pencil team, like fluidx) advects b_y (stage A, velocity
-//     averaged with the j-1 pencil) and b_z (stage B, with the k-1 pencil) in
-//     the same pass, writes them in place, and writes the shifted fluxes
-//     sA(i,j,k) = fluxA(i-1,j,k), sB(i,j,k) = fluxB(i-1,j,k) to caller scratch;
-//   kernel 2 (one thread per cell) gathers
-//     b_x = (((b_x - sA(j)) + sA(j+1)) - sB(k)) + sB(k+1),
+//   kernel 1 (per pencil team, like fluidx) advects frame b(2) (stage A,
+//     velocity averaged with the j-1 pencil) and b(3) (stage B, with the k-1
+//     pencil) in the same pass, writes them in place, and writes the shifted
+//     fluxes sA(i,j,k) = fluxA(i-1,j,k), sB(i,j,k) = fluxB(i-1,j,k) to scratch
+//     indexed like the stored cells;
+//   kernel 2 (one thread per stored cell) gathers
+//     b(1) = (((b(1) - sA(j)) + sA(j+1)) - sB(k)) + sB(k+1),
 //   which is the reference's per-cell rounding order (A1, A2, B1, B2).
-// Stage B reads only the pre-advection b_z and u, so fusing A and B in one
-// kernel changes no value.
+// Stage B reads only the pre-advection b(3) and u, so fusing A and B in one
+// kernel changes no value.  Pencils that run across memory (the y and z
+// sweeps of an x-major box) are staged through shared memory in rows, as in
+// fluidx_kernel.cuh.
 #include "kernels.cuh"
 
 namespace mhd {
 
-// one exchange buffer holds 4 floats per cell; two alternate
-__host__ __device__ constexpr int advect_smem_floats_per_pencil(int n) { return 8 * n; }
+// shared floats: two alternating exchange buffers of 4 per cell and pencil,
+// plus, for pencils across memory, the row staging (rho and m of the j-1
+// column and the k-1 plane, own b(2) b(3); reused for the outputs)
+// Row staging layouts are [i][column] with odd row strides, so a warp reading
+// one column down consecutive cells hits 32 different banks.
+__host__ __device__ inline int ax_r2(int ppc) { return 2 * (ppc + 1) + 1; }   // U2 row
+__host__ __device__ inline int ax_rk(int ppc) { return 2 * ppc + 1; }         // UK, BO row
+__host__ __device__ inline int ax_ro(int ppc) { return 4 * ppc + 1; }         // output row
+__host__ __device__ inline long long ax_smem_floats(int n, int ppc, bool rows)
+{
+    long long s = 8LL * n * ppc;
+    if (rows) s += (long long)n * (ax_r2(ppc) + 2 * ax_rk(ppc));
+    return s;
+}
 
-template <int CPL, int WPP>
+template <int CPL, int WPP, class M, bool ROWS>
 __global__ void __launch_bounds__(256)
 advect_flux_kernel(AdvectArgs a)
 {
     constexpr int TPP = 32 * WPP;
     extern __shared__ float smem[];
-    const int n = a.f.n;
+    const Frame &f = a.f;
+    const int n = f.n;
     const int ppc = blockDim.x / TPP;
     const int q = threadIdx.x / TPP;
-    const long long pen = (long long)blockIdx.x * ppc + q;
-    const bool live = pen < a.f.npen;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+
+    long long pen = 0;
+    int j0 = 0, k = 0, nvalid = 0;
+    if (!ROWS) {
+        pen = (long long)blockIdx.x * ppc + q;
+    } else {
+        const int njb = (f.ny + ppc - 1) / ppc;
+        k = blockIdx.x / njb;
+        j0 = (blockIdx.x - k * njb) * ppc;
+        nvalid = min(ppc, f.ny - j0);
+    }
+    const bool live = ROWS ? q < nvalid : pen < f.npen;
     float *xa = smem + (size_t)q * 8 * n;  // buffer 0
     float *xb = xa + 4 * n;                // buffer 1
+    float *ST = smem + (size_t)ppc * 8 * n;
 
     Team<CPL, WPP> tm;
     tm.init(threadIdx.x - q * TPP, n);
     const float dt = *a.dt;
 
-    const int j = live ? (int)(pen % a.f.ny) : 0;
-    const int k = live ? (int)(pen / a.f.ny) : 0;
-    const int jm = (j == 0) ? a.f.ny - 1 : j - 1;
-    const int km = (k == 0) ? a.f.nz - 1 : k - 1;
-    const long long base = ((long long)k * a.f.ny + j) * n;
-    const long long bjm = ((long long)k * a.f.ny + jm) * n;
-    const long long bkm = ((long long)km * a.f.ny + j) * n;
-
-    // ---- per-cell velocity at the j-1/2 (A) and k-1/2 (B) faces ----
     float vA[CPL], vB[CPL], bA[CPL], bB[CPL];
+    long long base = 0;   // !ROWS: first stored cell of the pencil
+    if (!ROWS) {
+        const int j = live ? (int)(pen % f.ny) : 0;
+        const int kk = live ? (int)(pen / f.ny) : 0;
+        const int jm = (j == 0) ? f.ny - 1 : j - 1;
+        const int km = (kk == 0) ? f.nz - 1 : kk - 1;
+        base = ((long long)kk * f.ny + j) * n;
+        const long long bjm = ((long long)kk * f.ny + jm) * n;
+        const long long bkm = ((long long)km * f.ny + j) * n;
+        // vx = (m_x(jm) + m_x) / (rho(jm) + rho)  (A1.c:58, B1.c:51)
 #pragma unroll
-    for (int m = 0; m < CPL; ++m) {
-        const int c = tm.cell[m];
-        if (live && tm.valid[m]) {
-            const float r0 = a.u[(base + c) * 5 + 0], m0 = a.u[(base + c) * 5 + 1];
-            const float rj = a.u[(bjm + c) * 5 + 0], mj = a.u[(bjm + c) * 5 + 1];
-            const float rk = a.u[(bkm + c) * 5 + 0], mk = a.u[(bkm + c) * 5 + 1];
-            vA[m] = fdiv(fadd(mj, m0), fadd(rj, r0));
-            vB[m] = fdiv(fadd(mk, m0), fadd(rk, r0));
-            bA[m] = a.b[(base + c) * 3 + 1];
-            bB[m] = a.b[(base + c) * 3 + 2];
-        } else {
-            vA[m] = 0.0f; vB[m] = 0.0f; bA[m] = 0.0f; bB[m] = 0.0f;
+        for (int m = 0; m < CPL; ++m) {
+            const int c = tm.cell[m];
+            if (live && tm.valid[m]) {
+                const float r0 = a.u[(base + c) * 5 + 0], m0 = a.u[(base + c) * 5 + 1];
+                const float rj = a.u[(bjm + c) * 5 + 0], mj = a.u[(bjm + c) * 5 + 1];
+                const float rk = a.u[(bkm + c) * 5 + 0], mk = a.u[(bkm + c) * 5 + 1];
+                vA[m] = M::div(M::add(mj, m0), M::add(rj, r0));
+                vB[m] = M::div(M::add(mk, m0), M::add(rk, r0));
+                bA[m] = a.b[(base + c) * 3 + 1];
+                bB[m] = a.b[(base + c) * 3 + 2];
+            } else {
+                vA[m] = 0.0f; vB[m] = 0.0f; bA[m] = 0.0f; bB[m] = 0.0f;
+            }
         }
-        if (tm.valid[m]) { xa[c] = vA[m]; xa[n + c] = vB[m]; }
+    } else {
+        // rows of the tile: U2 = (rho, m) of columns j0-1 .. j0+nvalid-1 at k,
+        // UK = (rho, m) of columns j0 .. at k-1, BO = own (b(2), b(3))
+        float *U2 = ST;                                   // (ppc+1) * 2n
+        const int r2 = ax_r2(ppc), rk = ax_rk(ppc);
+        float *UK = U2 + (size_t)n * r2;                  // n * rk
+        float *BO = UK + (size_t)n * rk;                  // n * rk
+        const int km = (k == 0) ? f.nz - 1 : k - 1;
+        const long long kb = (long long)k * f.sk, kmb = (long long)km * f.sk;
+        const int pm = nib(f.pu, 1), p2 = nib(f.pb, 1), p3 = nib(f.pb, 2);
+        // per-lane column offsets (2*(ppc+1) <= 18 columns for ppc <= 8)
+        const int qq = lane >> 1, w = lane & 1;
+        const bool on2 = lane < 2 * (nvalid + 1), onk = lane < 2 * nvalid;
+        int jc = j0 - 1 + qq;
+        if (jc < 0) jc += f.ny;
+        if (jc >= f.ny) jc -= f.ny;
+        const int g2 = jc * 5 + (w ? pm : 0);
+        const int gk = (j0 + qq) * 5 + (w ? pm : 0);
+        const int gb = (j0 + qq) * 3 + (w ? p3 : p2);
+        for (int i = warp; i < n; i += nwarps) {
+            const long long rowc = kb + (long long)i * f.si;
+            const long long rowk = kmb + (long long)i * f.si;
+            if (on2) cp_async4(&U2[i * r2 + lane], a.u + rowc * 5 + g2);
+            if (onk) {
+                cp_async4(&UK[i * rk + lane], a.u + rowk * 5 + gk);
+                cp_async4(&BO[i * rk + lane], a.b + rowc * 3 + gb);
+            }
+        }
+        cp_async_wait_all();
+        __syncthreads();
+#pragma unroll
+        for (int m = 0; m < CPL; ++m) {
+            const int c = tm.cell[m];
+            if (live && tm.valid[m]) {
+                const float *uo = U2 + c * r2 + 2 * (q + 1), *uj = U2 + c * r2 + 2 * q;
+                const float *uk = UK + c * rk + 2 * q, *bo = BO + c * rk + 2 * q;
+                vA[m] = M::div(M::add(uj[1], uo[1]), M::add(uj[0], uo[0]));
+                vB[m] = M::div(M::add(uk[1], uo[1]), M::add(uk[0], uo[0]));
+                bA[m] = bo[0];
+                bB[m] = bo[1];
+            } else {
+                vA[m] = 0.0f; vB[m] = 0.0f; bA[m] = 0.0f; bB[m] = 0.0f;
+            }
+        }
     }
+#pragma unroll
+    for (int m = 0; m < CPL; ++m)
+        if (tm.valid[m]) { xa[tm.cell[m]] = vA[m]; xa[n + tm.cell[m]] = vB[m]; }
     tm.sync();
-    // vx = (cshift(vx,-1) + cshift(vx,1) + 2 vx)/4 ; the (s + 2vx)/4 is formed
-    // in double by the reference and rounded once: fma + exact quarter.
+    // vx = (cshift(vx,-1) + cshift(vx,1) + 2 vx)/4: the (s + 2vx)/4 is formed
+    // in double by the reference and rounded once; the quarter is exact.
     float gA[CPL], gB[CPL];   // smoothed velocities vg
 #pragma unroll
     for (int m = 0; m < CPL; ++m) {
-        const float sa = fadd(xa[tm.im[m]], xa[tm.ip[m]]);
-        const float sb = fadd(xa[n + tm.im[m]], xa[n + tm.ip[m]]);
-        gA[m] = 0.25f * ffma(2.0f, vA[m], sa);
-        gB[m] = 0.25f * ffma(2.0f, vB[m], sb);
+        const float sa = M::add(xa[tm.im[m]], xa[tm.ip[m]]);
+        const float sb = M::add(xa[n + tm.im[m]], xa[n + tm.ip[m]]);
+        gA[m] = 0.25f * M::twice_plus(vA[m], sa);
+        gB[m] = 0.25f * M::twice_plus(vB[m], sb);
         if (tm.valid[m]) {
             const int c = tm.cell[m];
             xb[c] = gA[m]; xb[n + c] = gB[m];
-            xb[2 * n + c] = fmul(bA[m], gA[m]);
-            xb[3 * n + c] = fmul(bB[m], gB[m]);
+            xb[2 * n + c] = M::mul(bA[m], gA[m]);
+            xb[3 * n + c] = M::mul(bB[m], gB[m]);
         }
     }
     tm.sync();
-    // tvdb: vh = (vg + cshift(vg,1))/2 ; flux1 = b vg (upwind by vh)
+    // tvdb: vh = (vg + cshift(vg,1))/2 ; flux1 = b vg, upwinded by vh
     float hA[CPL], hB[CPL], f1A[CPL], f1B[CPL];
 #pragma unroll
     for (int m = 0; m < CPL; ++m) {
         const int c = tm.cell[m], cp = tm.ip[m];
-        hA[m] = fadd(0.5f * gA[m], 0.5f * xb[cp]);
-        hB[m] = fadd(0.5f * gB[m], 0.5f * xb[n + cp]);
+        hA[m] = M::add(0.5f * gA[m], 0.5f * xb[cp]);
+        hB[m] = M::add(0.5f * gB[m], 0.5f * xb[n + cp]);
         f1A[m] = (hA[m] > 0.0f) ? xb[2 * n + c] : xb[2 * n + cp];
         f1B[m] = (hB[m] > 0.0f) ? xb[3 * n + c] : xb[3 * n + cp];
         if (tm.valid[m]) { xa[c] = f1A[m]; xa[n + c] = f1B[m]; }
     }
     tm.sync();
     // b1 = b - (flux1 - cshift(flux1,-1)) dt/2 : the product is float, the
-    // halving and the subtraction are double in the reference -> one rounding.
+    // halving and the subtraction double in the reference -> one rounding.
     // Then exchange the products vg*b1.
 #pragma unroll
     for (int m = 0; m < CPL; ++m) {
         const int cm = tm.im[m];
-        const float b1A = ffma(-0.5f, fmul(fsub(f1A[m], xa[cm]), dt), bA[m]);
-        const float b1B = ffma(-0.5f, fmul(fsub(f1B[m], xa[n + cm]), dt), bB[m]);
+        const float b1A = M::minus_half(bA[m], M::mul(M::sub(f1A[m], xa[cm]), dt));
+        const float b1B = M::minus_half(bB[m], M::mul(M::sub(f1B[m], xa[n + cm]), dt));
         if (tm.valid[m]) {
             const int c = tm.cell[m];
-            xb[c] = fmul(gA[m], b1A);
-            xb[n + c] = fmul(gB[m], b1B);
+            xb[c] = M::mul(gA[m], b1A);
+            xb[n + c] = M::mul(gB[m], b1B);
         }
     }
     tm.sync();
-    // upwind second-order flux on the right face with van Leer limiting
+    // upwind second-order flux on the right face with the van Leer limiter;
+    // wp, wm are half differences, so the slope of the undivided ones is
+    // 2 wm wp/(wm+wp) exactly (tvdb.c:64-75)
     float flA[CPL], flB[CPL];
 #pragma unroll
     for (int m = 0; m < CPL; ++m) {
@@ -120,58 +198,92 @@ advect_flux_kernel(AdvectArgs a)
         for (int s = 0; s < 2; ++s) {
             const float *g = xb + s * n;
             const float h = s ? hB[m] : hA[m];
-            float w, wp, wm;
+            float w, Wp, Wm;
             if (h > 0.0f) {
                 w = g[c];
-                wp = 0.5f * fsub(g[cp], w);
-                wm = 0.5f * fsub(w, g[cm]);
+                Wp = M::sub(g[cp], w);
+                Wm = M::sub(w, g[cm]);
             } else {
                 w = g[cp];
-                wp = 0.5f * fsub(w, g[cpp]);
-                wm = 0.5f * fsub(g[c], w);
+                Wp = M::sub(w, g[cpp]);
+                Wm = M::sub(g[c], w);
             }
-            const float dw = van_leer(wm, wp);
-            const float fl = fmul(fadd(w, dw), dt);
+            const float dw = M::slope(Wm, Wp);
+            const float fl = M::mul(M::add(w, dw), dt);
             if (s) flB[m] = fl; else flA[m] = fl;
         }
         if (tm.valid[m]) { xa[2 * n + c] = flA[m]; xa[3 * n + c] = flB[m]; }
     }
     tm.sync();
-    // b = b - (flux - cshift(flux,-1)) ; store b_y, b_z and the shifted flux
+    // b = b - (flux - cshift(flux,-1)) ; outputs b(2), b(3), sA, sB
+    if (!ROWS) {
 #pragma unroll
-    for (int m = 0; m < CPL; ++m) {
-        if (live && tm.valid[m]) {
-            const int c = tm.cell[m], cm = tm.im[m];
+        for (int m = 0; m < CPL; ++m) {
+            if (live && tm.valid[m]) {
+                const int c = tm.cell[m], cm = tm.im[m];
+                const float sa = xa[2 * n + cm], sb = xa[3 * n + cm];
+                a.b[(base + c) * 3 + 1] = M::sub(bA[m], M::sub(flA[m], sa));
+                a.b[(base + c) * 3 + 2] = M::sub(bB[m], M::sub(flB[m], sb));
+                a.sA[base + c] = sa;
+                a.sB[base + c] = sb;
+            }
+        }
+    } else {
+        float o[CPL][4];
+#pragma unroll
+        for (int m = 0; m < CPL; ++m) {
+            const int cm = tm.im[m];
             const float sa = xa[2 * n + cm], sb = xa[3 * n + cm];
-            a.b[(base + c) * 3 + 1] = fsub(bA[m], fsub(flA[m], sa));
-            a.b[(base + c) * 3 + 2] = fsub(bB[m], fsub(flB[m], sb));
-            a.sA[base + c] = sa;
-            a.sB[base + c] = sb;
+            o[m][0] = M::sub(bA[m], M::sub(flA[m], sa));
+            o[m][1] = M::sub(bB[m], M::sub(flB[m], sb));
+            o[m][2] = sa;
+            o[m][3] = sb;
+        }
+        const int ro = ax_ro(ppc);
+        float *OUT = ST;   // n * ro: row i holds (b(2), b(3), sA, sB) of each pencil
+        __syncthreads();   // the row staging is consumed
+#pragma unroll
+        for (int m = 0; m < CPL; ++m)
+            if (live && tm.valid[m])
+#pragma unroll
+                for (int w = 0; w < 4; ++w) OUT[tm.cell[m] * ro + 4 * q + w] = o[m][w];
+        __syncthreads();
+        const long long kb = (long long)k * f.sk;
+        const int p2 = nib(f.pb, 1), p3 = nib(f.pb, 2);
+        const int qq = lane >> 2, w = lane & 3;      // 4*ppc <= 32 values per row
+        const bool on = lane < 4 * nvalid;
+        for (int i = warp; i < n; i += nwarps) {
+            if (!on) continue;
+            const long long cell = kb + (long long)i * f.si + j0 + qq;
+            const float v = OUT[i * ro + lane];
+            if (w == 0) a.b[cell * 3 + p2] = v;
+            else if (w == 1) a.b[cell * 3 + p3] = v;
+            else if (w == 2) a.sA[cell] = v;
+            else a.sB[cell] = v;
         }
     }
 }
 
-// b_x(i,j,k) = (((b_x - sA(i,j,k)) + sA(i,j+1,k)) - sB(i,j,k)) + sB(i,j,k+1)
+// b(1) = (((b(1) - sA(i,j,k)) + sA(i,j+1,k)) - sB(i,j,k)) + sB(i,j,k+1), one
+// thread per stored cell; j, k and the neighbours follow the frame's strides.
 __global__ void __launch_bounds__(256)
-advect_bx_kernel(float *__restrict__ b, const float *__restrict__ sA, const float *__restrict__ sB,
+advect_b1_kernel(float *__restrict__ b, const float *__restrict__ sA, const float *__restrict__ sB,
                  Frame f, long long ncell)
 {
     const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= ncell) return;
-    const long long pen = c / f.n;
-    const int i = (int)(c - pen * f.n);
-    const int j = (int)(pen % f.ny);
-    const int k = (int)(pen / f.ny);
-    const int jp = (j + 1 == f.ny) ? 0 : j + 1;
-    const int kp = (k + 1 == f.nz) ? 0 : k + 1;
-    const long long cj = ((long long)k * f.ny + jp) * f.n + i;
-    const long long ck = ((long long)kp * f.ny + j) * f.n + i;
-    float bx = b[c * 3];
+    const unsigned cu = (unsigned)c;   // ncell < 2^31
+    const int j = (int)((cu / (unsigned)f.sj) % (unsigned)f.ny);
+    const int k = (int)((cu / (unsigned)f.sk) % (unsigned)f.nz);
+    const long long cj = c + ((j + 1 == f.ny) ? -(long long)(f.ny - 1) * f.sj : f.sj);
+    const long long ck = c + ((k + 1 == f.nz) ? -(long long)(f.nz - 1) * f.sk : f.sk);
+    const int p1 = nib(f.pb, 0);
+    float bx = b[c * 3 + p1];
     bx = fsub(bx, sA[c]);
     bx = fadd(bx, sA[cj]);
     bx = fsub(bx, sB[c]);
     bx = fadd(bx, sB[ck]);
-    b[c * 3] = bx;
+    b[c * 3 + p1] = bx;
 }
 
 PencilCfg advect_pick(int n)
@@ -184,36 +296,47 @@ PencilCfg advect_pick(int n)
     return {4, 8, 1};
 }
 
-cudaError_t launch_advect(const AdvectArgs &a, const PencilCfg &cfg, cudaStream_t s)
+template <int CPL, int WPP, class M, bool ROWS>
+static cudaError_t launch_advect_inst(const AdvectArgs &a, int ppc, cudaStream_t s)
 {
-    const int tpp = 32 * cfg.wpp;
-    const int threads = tpp * cfg.ppc;
-    const long long blocks = (a.f.npen + cfg.ppc - 1) / cfg.ppc;
-    const size_t smem = sizeof(float) * (size_t)cfg.ppc * advect_smem_floats_per_pencil(a.f.n);
-    cudaError_t e = cudaErrorInvalidConfiguration;
-#define MHD_ADVECT_CASE(C, W)                                                                  \
-    if (cfg.cpl == C && cfg.wpp == W) {                                                        \
-        static int smem_set_##C##_##W = 0;                                                     \
-        if (smem > 48 * 1024 && (size_t)smem_set_##C##_##W < smem) {                           \
-            e = cudaFuncSetAttribute(advect_flux_kernel<C, W>,                                 \
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);  \
-            if (e != cudaSuccess) return e;                                                    \
-            smem_set_##C##_##W = (int)smem;                                                    \
-        }                                                                                      \
-        advect_flux_kernel<C, W><<<(unsigned)blocks, threads, smem, s>>>(a);                   \
-        e = cudaGetLastError();                                                                \
+    static size_t smem_set = 0;
+    const int threads = 32 * WPP * ppc;
+    const long long blocks = ROWS ? (long long)((a.f.ny + ppc - 1) / ppc) * a.f.nz
+                                  : (a.f.npen + ppc - 1) / ppc;
+    const size_t smem = sizeof(float) * (size_t)ax_smem_floats(a.f.n, ppc, ROWS);
+    if (smem > 227 * 1024) return cudaErrorInvalidConfiguration;
+    if (smem > 48 * 1024 && smem_set < smem) {
+        cudaError_t e = cudaFuncSetAttribute(advect_flux_kernel<CPL, WPP, M, ROWS>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        smem_set = smem;
     }
-    MHD_ADVECT_CASE(1, 1)
-    else MHD_ADVECT_CASE(2, 1)
-    else MHD_ADVECT_CASE(4, 1)
-    else MHD_ADVECT_CASE(4, 2)
-    else MHD_ADVECT_CASE(4, 4)
-    else MHD_ADVECT_CASE(4, 8)
-#undef MHD_ADVECT_CASE
+    advect_flux_kernel<CPL, WPP, M, ROWS><<<(unsigned)blocks, threads, smem, s>>>(a);
+    return cudaGetLastError();
+}
+
+template <class M>
+static cudaError_t launch_advect_policy(const AdvectArgs &a, const PencilCfg &cfg, cudaStream_t s)
+{
+    const bool rows = a.f.si != 1;
+#define MHD_AX(C, W)                                                                  \
+    if (cfg.cpl == C && cfg.wpp == W)                                                 \
+        return rows ? launch_advect_inst<C, W, M, true>(a, cfg.ppc, s)                \
+                    : launch_advect_inst<C, W, M, false>(a, cfg.ppc, s);
+    MHD_PENCIL_SHAPES(MHD_AX)
+#undef MHD_AX
+    return cudaErrorInvalidConfiguration;
+}
+
+cudaError_t launch_advect(const AdvectArgs &a, const PencilCfg &cfg, int math, cudaStream_t s)
+{
+    if (!pencil_shape_ok(cfg, a.f.n) || !frame_supported(a.f)) return cudaErrorInvalidConfiguration;
+    cudaError_t e = (math == MHD_MATH_FAST) ? launch_advect_policy<Fast>(a, cfg, s)
+                                            : launch_advect_policy<Faithful>(a, cfg, s);
     if (e != cudaSuccess) return e;
     const long long ncell = a.f.npen * a.f.n;
     const long long nb = (ncell + 255) / 256;
-    advect_bx_kernel<<<(unsigned)nb, 256, 0, s>>>(a.b, a.sA, a.sB, a.f, ncell);
+    advect_b1_kernel<<<(unsigned)nb, 256, 0, s>>>(a.b, a.sA, a.sB, a.f, ncell);
     return cudaGetLastError();
 }
 

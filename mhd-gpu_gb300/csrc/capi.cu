@@ -91,7 +91,7 @@ int mhdgpu_fluidx(float *u_out, const float *u_in, const float *b, int nx, int n
         return fail(MHD_ERR_ARG, "mhdgpu_fluidx: u_out partially overlaps u_in");
     FluidxArgs a{u_out, u_in, b, d_dt, d_health, make_frame(nx, ny, nz)};
     ProfScope ps(MHD_KCLASS_FLUIDX, 1, (cudaStream_t)stream);
-    MHD_CU(launch_fluidx(a, fluidx_pick(nx), (cudaStream_t)stream), "mhdgpu_fluidx");
+    MHD_CU(launch_fluidx(a, pencil_cfg(MHD_KCLASS_FLUIDX, nx), math_mode(), (cudaStream_t)stream), "mhdgpu_fluidx");
     return MHD_OK;
 }
 
@@ -110,7 +110,7 @@ int mhdgpu_advectbyzx(float *b, const float *u, int nx, int ny, int nz, const fl
     const long long ncell = (long long)nx * ny * nz;
     AdvectArgs a{b, u, d_dt, d_scratch, d_scratch + ncell, make_frame(nx, ny, nz)};
     ProfScope ps(MHD_KCLASS_ADVECT, 2, (cudaStream_t)stream);
-    MHD_CU(launch_advect(a, advect_pick(nx), (cudaStream_t)stream), "mhdgpu_advectbyzx");
+    MHD_CU(launch_advect(a, pencil_cfg(MHD_KCLASS_ADVECT, nx), math_mode(), (cudaStream_t)stream), "mhdgpu_advectbyzx");
     return MHD_OK;
 }
 
@@ -227,15 +227,64 @@ int mhdgpu_step(float *u, float *b, int nx, int ny, int nz, const float *d_dt, v
     return sweep(u, b, nx, ny, nz, d_dt, scr, d_health, false, s);
 }
 
+// one sweep pair on a frame view of the x-major state: fluid then field, or
+// field then fluid; launches the kernels on the view directly
+static int sweep_view(float *u, float *b, const Frame &f, const float *dt, float *scr,
+                      unsigned *health, bool fluid_first, cudaStream_t s)
+{
+    const long long ncell = f.npen * f.n;
+    FluidxArgs fa{u, u, b, dt, health, f};
+    AdvectArgs aa{b, u, dt, scr, scr + ncell, f};
+    for (int part = 0; part < 2; ++part) {
+        if ((part == 0) == fluid_first) {
+            ProfScope ps(MHD_KCLASS_FLUIDX, 1, s);
+            MHD_CU(launch_fluidx(fa, pencil_cfg(MHD_KCLASS_FLUIDX, f.n, f.si != 1), math_mode(), s),
+                   "fused fluidx");
+        } else {
+            ProfScope ps(MHD_KCLASS_ADVECT, 2, s);
+            MHD_CU(launch_advect(aa, pencil_cfg(MHD_KCLASS_ADVECT, f.n, f.si != 1), math_mode(), s),
+                   "fused advectbyzx");
+        }
+    }
+    return MHD_OK;
+}
+
+size_t mhdgpu_step_fused_workspace_bytes(int nx, int ny, int nz)
+{
+    if (!dims_ok(nx, ny, nz) || ny > MHD_MAX_PENCIL || nz > MHD_MAX_PENCIL) return 0;
+    return sizeof(float) * 2 * (size_t)nx * ny * nz;
+}
+
+int mhdgpu_step_fused(float *u, float *b, int nx, int ny, int nz, const float *d_dt, void *d_work,
+                      unsigned *d_health, mhdgpu_stream_t stream)
+{
+    int st = check_dims(nx, ny, nz, "mhdgpu_step_fused");
+    if (st) return st;
+    if (ny > MHD_MAX_PENCIL || nz > MHD_MAX_PENCIL)
+        return fail(MHD_ERR_ARG, "mhdgpu_step_fused: every axis becomes a pencil; each must be <= MHD_MAX_PENCIL");
+    if (!u || !b || !d_dt || !d_work) return fail(MHD_ERR_ARG, "mhdgpu_step_fused: null pointer");
+    cudaStream_t s = (cudaStream_t)stream;
+    float *scr = (float *)d_work;
+    const Frame fx = make_view(0, nx, ny, nz), fy = make_view(1, nx, ny, nz), fz = make_view(2, nx, ny, nz);
+    if ((st = sweep_view(u, b, fx, d_dt, scr, d_health, true, s))) return st;
+    if ((st = sweep_view(u, b, fy, d_dt, scr, d_health, true, s))) return st;
+    if ((st = sweep_view(u, b, fz, d_dt, scr, d_health, true, s))) return st;
+    if ((st = sweep_view(u, b, fz, d_dt, scr, d_health, false, s))) return st;
+    if ((st = sweep_view(u, b, fy, d_dt, scr, d_health, false, s))) return st;
+    return sweep_view(u, b, fx, d_dt, scr, d_health, false, s);
+}
+
 int mhdgpu_advance(float *u, float *b, int nx, int ny, int nz, int nsteps, double cfl_number,
                    int cfl_mode, float tf, mhdgpu_clock *d_clock, float *d_dt_log, void *d_work,
-                   mhdgpu_stream_t stream)
+                   int path, mhdgpu_stream_t stream)
 {
     if (nsteps < 0) return fail(MHD_ERR_ARG, "mhdgpu_advance: nsteps < 0");
     if (!d_clock) return fail(MHD_ERR_ARG, "mhdgpu_advance: null clock");
     if (!(cfl_number > 0.0)) return fail(MHD_ERR_ARG, "mhdgpu_advance: cfl_number must be > 0");
     if (cfl_mode != MHD_CFL_C && cfl_mode != MHD_CFL_AVERAGED)
         return fail(MHD_ERR_ARG, "mhdgpu_advance: bad cfl mode");
+    if (path != MHD_PATH_PLAIN && path != MHD_PATH_FUSED)
+        return fail(MHD_ERR_ARG, "mhdgpu_advance: bad path");
     cudaStream_t s = (cudaStream_t)stream;
     for (int it = 0; it < nsteps; ++it) {
         {
@@ -243,21 +292,26 @@ int mhdgpu_advance(float *u, float *b, int nx, int ny, int nz, int nsteps, doubl
             MHD_CU(launch_cfl(u, b, nx, ny, nz, cfl_mode, &d_clock->cmax, s), "mhdgpu_advance");
             MHD_CU(launch_clock(d_clock, cfl_number, tf, d_dt_log, s), "mhdgpu_advance");
         }
-        int st = mhdgpu_step(u, b, nx, ny, nz, &d_clock->dt, d_work, &d_clock->health, stream);
+        int st = (path == MHD_PATH_FUSED)
+                     ? mhdgpu_step_fused(u, b, nx, ny, nz, &d_clock->dt, d_work, &d_clock->health, stream)
+                     : mhdgpu_step(u, b, nx, ny, nz, &d_clock->dt, d_work, &d_clock->health, stream);
         if (st) return st;
     }
     return MHD_OK;
 }
 
 int mhdgpu_run_host(float *u, float *b, int nx, int ny, int nz, double cfl_number, int cfl_mode,
-                    float *t, float tf, int max_steps, float *dt_log, int *steps_done)
+                    float *t, float tf, int max_steps, float *dt_log, int *steps_done, int path)
 {
     int st = check_dims(nx, ny, nz, "mhdgpu_run_host");
     if (st) return st;
     if (!u || !b || !t) return fail(MHD_ERR_ARG, "mhdgpu_run_host: null pointer");
     if (max_steps < 0) return fail(MHD_ERR_ARG, "mhdgpu_run_host: max_steps < 0");
+    if (path != MHD_PATH_PLAIN && path != MHD_PATH_FUSED)
+        return fail(MHD_ERR_ARG, "mhdgpu_run_host: bad path");
     const size_t ncell = (size_t)nx * ny * nz;
-    const size_t wbytes = mhdgpu_step_workspace_bytes(nx, ny, nz);
+    const size_t wbytes = path == MHD_PATH_FUSED ? mhdgpu_step_fused_workspace_bytes(nx, ny, nz)
+                                                 : mhdgpu_step_workspace_bytes(nx, ny, nz);
     if (!wbytes) return fail(MHD_ERR_ARG, "mhdgpu_run_host: box too large for the step");
     float *du = nullptr, *db = nullptr, *dlog = nullptr;
     void *dw = nullptr;
@@ -280,7 +334,7 @@ int mhdgpu_run_host(float *u, float *b, int nx, int ny, int nz, double cfl_numbe
         RH(cudaMemcpyAsync(du, u, ncell * 5 * sizeof(float), cudaMemcpyHostToDevice, s), "mhdgpu_run_host: upload");
         RH(cudaMemcpyAsync(db, b, ncell * 3 * sizeof(float), cudaMemcpyHostToDevice, s), "mhdgpu_run_host: upload");
         ret = mhdgpu_advance(du, db, nx, ny, nz, max_steps, cfl_number, cfl_mode, tf, dclk, dlog, dw,
-                             (mhdgpu_stream_t)s);
+                             path, (mhdgpu_stream_t)s);
         if (ret) goto done;
         RH(cudaMemcpyAsync(u, du, ncell * 5 * sizeof(float), cudaMemcpyDeviceToHost, s), "mhdgpu_run_host: download");
         RH(cudaMemcpyAsync(b, db, ncell * 3 * sizeof(float), cudaMemcpyDeviceToHost, s), "mhdgpu_run_host: download");

@@ -1,0 +1,372 @@
+// fluidx_kernel.cuh - the fluid sweep (relaxing TVD, RK2) on pencils of a
+// frame view, for sm_103a.  Instantiated per math policy and staging mode in
+// fluidx.cu (faithful) and fluidx_fast.cu (fast).
+//
+// Algorithm: Heterogeneous_MHD/C/fluidx.c:19-102 (gather + cell-centred B),
+// tvd1.c:8-118 (RK2 half and full step, van Leer limiter), mhdflux.c:9-72
+// (flux vector and pencil-wide max fast speed).
+//
+// GB300 mapping.  A CTA owns PPC pencils and stages their u into shared
+// memory (US), where it stays for the whole update and receives the result;
+// registers hold only the cell-centred B, the half-step state and the fluxes
+// of the cells a thread owns.  Two staging modes:
+//   ROWS = false: the pencils are contiguous (si = 1: the reference layout, or
+//     the x sweep of an x-major box); the CTA's pencils are consecutive, so u
+//     and b are single contiguous chunks moved with 16-byte accesses;
+//   ROWS = true: the pencils run across memory (sj = 1: the y and z sweeps of
+//     an x-major box, read in place instead of after a transpose); the CTA owns
+//     PPC neighbouring pencils at one k, so each cell i of them is one
+//     contiguous row of PPC cells, and rows are moved with consecutive lanes
+//     on consecutive addresses (the transpose happens in shared memory).
+// Each pencil belongs to a team of 32*WPP threads, CPL cells per thread
+// (cell c = m*32*WPP + t).  Stencil neighbours (i-1, i+1, i+2) go through a
+// per-pencil shared buffer; the two pencil-wide maxima of the fast speed are
+// warp-shuffle reductions (plus one shared step when WPP > 1).  No tensor
+// cores: nothing on this path is a contraction; the kernel is bounded by FP32
+// issue.
+#pragma once
+
+#include "kernels.cuh"
+
+namespace mhd {
+
+// shared-memory geometry (floats), shared by the kernel and its launcher
+__host__ __device__ inline int fx_ps(int n, bool rows)          // u stride per pencil
+{
+    return rows ? 5 * n + ((37 - (5 * n) % 32) % 32) : 5 * n;   // = 5 (mod 32) for rows
+}
+__host__ __device__ inline int fx_bs(int n) { return 3 * n + ((35 - (3 * n) % 32) % 32); }
+__host__ __device__ inline long long fx_xsize(int n, int ppc, bool rows)
+{
+    long long x = 10LL * n * ppc;
+    if (rows) {
+        const long long need = (long long)(ppc + 1) * fx_bs(n) + (long long)(ppc + 1) * n;
+        if (need > x) x = need;
+    }
+    return x;
+}
+__host__ __device__ inline long long fx_smem_floats(int n, int ppc, int wpp, bool rows)
+{
+    return (long long)ppc * fx_ps(n, rows) + fx_xsize(n, ppc, rows) + (long long)ppc * wpp;
+}
+
+template <int CPL, int WPP, class M, bool ROWS>
+__global__ void __launch_bounds__(256)
+fluidx_kernel(FluidxArgs a)
+{
+    constexpr int TPP = 32 * WPP;
+    extern __shared__ float smem[];
+    const Frame &f = a.f;
+    const int n = f.n;
+    const int ppc = blockDim.x / TPP;
+    const int q = threadIdx.x / TPP;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    const int ps = fx_ps(n, ROWS);
+
+    // pencils of this CTA
+    long long p0 = 0;          // !ROWS: first linear pencil
+    int j0 = 0, k = 0;         // ROWS: first j and the plane
+    int nvalid;
+    if (!ROWS) {
+        p0 = (long long)blockIdx.x * ppc;
+        nvalid = (int)min((long long)ppc, f.npen - p0);
+    } else {
+        const int njb = (f.ny + ppc - 1) / ppc;
+        k = blockIdx.x / njb;
+        j0 = (blockIdx.x - k * njb) * ppc;
+        nvalid = min(ppc, f.ny - j0);
+    }
+    const bool live = q < nvalid;
+    const int jq = ROWS ? j0 + q : (live ? (int)((p0 + q) % f.ny) : 0);
+    const int kq = ROWS ? k : (live ? (int)((p0 + q) / f.ny) : 0);
+
+    float *US = smem;                                       // ppc * ps
+    float *XA = smem + (size_t)ppc * ps;                    // fx_xsize
+    float *red = XA + fx_xsize(n, ppc, ROWS);               // ppc * WPP
+    float *us = US + (size_t)q * ps;
+    float *x = XA + (size_t)q * 10 * n;
+    float *rq = red + q * WPP;
+
+    Team<CPL, WPP> tm;
+    tm.init(threadIdx.x - q * TPP, n);
+    const float dt = *a.dt;
+
+    // ---- stage u (kept) and b (transient) ----
+    float bc[CPL][3];
+    if (!ROWS) {
+        block_copy_in(US, a.u_in + p0 * 5 * n, (long long)nvalid * 5 * n, threadIdx.x, blockDim.x);
+        block_copy_in(XA, a.b + p0 * 3 * n, (long long)nvalid * 3 * n, threadIdx.x, blockDim.x);
+        __syncthreads();
+        // b3x = b/2 ; b3x(1) += cshift(b3x(1),1) ; b3x(2) += b(2,jp)/2 ;
+        // b3x(3) += b(3,kp)/2   (fluidx.c:71-81; the halvings are exact)
+        const int jp = (jq + 1 == f.ny) ? 0 : jq + 1;
+        const int kp = (kq + 1 == f.nz) ? 0 : kq + 1;
+        const float *bjp = a.b + ((long long)kq * f.ny + jp) * 3 * n;
+        const float *bkp = a.b + ((long long)kp * f.ny + jq) * 3 * n;
+        const float *pb = XA + (size_t)q * 3 * n;
+#pragma unroll
+        for (int m = 0; m < CPL; ++m) {
+            const int c = tm.cell[m];
+            if (live && tm.valid[m]) {
+                bc[m][0] = fadd(0.5f * pb[c * 3 + 0], 0.5f * pb[tm.ip[m] * 3 + 0]);
+                bc[m][1] = fadd(0.5f * pb[c * 3 + 1], 0.5f * __ldg(bjp + c * 3 + 1));
+                bc[m][2] = fadd(0.5f * pb[c * 3 + 2], 0.5f * __ldg(bkp + c * 3 + 2));
+            } else {
+                bc[m][0] = 0.0f; bc[m][1] = 0.0f; bc[m][2] = 0.0f;
+            }
+        }
+    } else {
+        const long long kb = (long long)k * f.sk;
+        const int kp = (k + 1 == f.nz) ? 0 : k + 1;
+        const long long kpb = (long long)kp * f.sk;
+        const int bs = fx_bs(n);
+        const int ks = ppc + 1;                          // SK row stride (odd for ppc = 2^m)
+        float *SB = XA;                                  // (ppc+1) * bs: frame b of columns j0..j0+nvalid
+        float *SK = XA + (size_t)(ppc + 1) * bs;         // n * ks: frame b(3) of plane k+1, [i][q]
+        const int ru = 5 * nvalid, rb = 3 * (nvalid + 1);
+        const int pb2 = nib(f.pb, 2);
+        // Per-lane offsets do not depend on the row: a row of u is ru floats
+        // at u_in + (rowc + j0)*5, element r -> pencil r/5, component r%5.
+        // (ru <= 40, rb <= 27 for ppc <= 8: at most two elements per lane.)
+        int us_off[2], sb_off[2], gb_off[2];
+        bool us_on[2], sb_on[2];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int r = lane + 32 * h;
+            us_on[h] = r < ru;
+            const int qq = r / 5, p = r - qq * 5;
+            us_off[h] = qq * ps + nib(f.iu, p);
+            sb_on[h] = r < rb;
+            const int qb = r / 3, pp = r - qb * 3;
+            int j = j0 + qb;
+            if (j >= f.ny) j -= f.ny;
+            sb_off[h] = qb * bs + nib(f.ib, pp);
+            gb_off[h] = j * 3 + pp;
+        }
+        const bool sk_on = lane < nvalid;
+        for (int i = warp; i < n; i += nwarps) {
+            const long long rowc = kb + (long long)i * f.si;    // cell of (i, 0, k)
+            const float *gu = a.u_in + (rowc + j0) * 5;
+            const float *gb = a.b + rowc * 3;
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                if (us_on[h]) cp_async4(&US[us_off[h] + i * 5], gu + lane + 32 * h);
+                if (sb_on[h]) cp_async4(&SB[sb_off[h] + i * 3], gb + gb_off[h]);
+            }
+            if (sk_on)
+                cp_async4(&SK[i * ks + lane], a.b + (kpb + (long long)i * f.si + j0 + lane) * 3 + pb2);
+        }
+        cp_async_wait_all();
+        __syncthreads();
+        const float *sb0 = SB + (size_t)q * bs, *sb1 = SB + (size_t)(q + 1) * bs;
+#pragma unroll
+        for (int m = 0; m < CPL; ++m) {
+            const int c = tm.cell[m];
+            if (live && tm.valid[m]) {
+                bc[m][0] = fadd(0.5f * sb0[c * 3 + 0], 0.5f * sb0[tm.ip[m] * 3 + 0]);
+                bc[m][1] = fadd(0.5f * sb0[c * 3 + 1], 0.5f * sb1[c * 3 + 1]);
+                bc[m][2] = fadd(0.5f * sb0[c * 3 + 2], 0.5f * SK[c * ks + q]);
+            } else {
+                bc[m][0] = 0.0f; bc[m][1] = 0.0f; bc[m][2] = 0.0f;
+            }
+        }
+    }
+    __syncthreads();   // the exchange area of one pencil overlaps the staged b of others
+
+    const float hdt = 0.5f * dt;
+    unsigned bad = 0;
+    float u1[CPL][5];
+
+    // ================= half step =================
+    {
+        float v[CPL][5];
+        float cl = 0.0f;
+#pragma unroll
+        for (int m = 0; m < CPL; ++m) {
+            float uu[5];
+            if (tm.valid[m] && live) {
+#pragma unroll
+                for (int ii = 0; ii < 5; ++ii) uu[ii] = us[tm.cell[m] * 5 + ii];
+            } else {
+                uu[0] = 1.0f; uu[1] = 0.0f; uu[2] = 0.0f; uu[3] = 0.0f; uu[4] = 1.0f;
+            }
+            float cs, p;
+            cell_flux<M>(uu, bc[m], v[m], cs, p);
+            if (tm.valid[m]) cl = fmaxf(cl, cs);
+        }
+        const float c = tm.pencil_max(cl, rq);
+        const bool cpos = c > 0.0f;
+        const float yc = cpos ? M::recip(c) : 0.0f;
+        // fr = c(u + v/c) kept in u1[]; wl = u - v/c exchanged in x[0:5n)
+#pragma unroll
+        for (int m = 0; m < CPL; ++m)
+#pragma unroll
+            for (int ii = 0; ii < 5; ++ii) {
+                const float uu = us[tm.cell[m] * 5 + ii];
+                const float vv = cpos ? M::divy(v[m][ii], c, yc) : v[m][ii];
+                u1[m][ii] = M::mul(c, M::add(uu, vv));
+                if (tm.valid[m]) x[ii * n + tm.cell[m]] = M::sub(uu, vv);
+            }
+        tm.sync();
+        // flux = (fr - c*cshift(wl,+1))/2, exchanged in x[5n:10n)
+#pragma unroll
+        for (int m = 0; m < CPL; ++m)
+#pragma unroll
+            for (int ii = 0; ii < 5; ++ii) {
+                const float fl = M::mul(c, x[ii * n + tm.ip[m]]);
+                u1[m][ii] = 0.5f * M::sub(u1[m][ii], fl);
+                if (tm.valid[m]) x[(5 + ii) * n + tm.cell[m]] = u1[m][ii];
+            }
+        tm.sync();
+        // u1 = u - (flux - cshift(flux,-1)) dt/2
+#pragma unroll
+        for (int m = 0; m < CPL; ++m)
+#pragma unroll
+            for (int ii = 0; ii < 5; ++ii) {
+                const float d = M::sub(u1[m][ii], x[(5 + ii) * n + tm.im[m]]);
+                u1[m][ii] = M::add(us[tm.cell[m] * 5 + ii], M::mul(-hdt, d));
+            }
+    }
+    tm.sync();   // every read of x[5n:10n) is done before it is rewritten
+
+    // ================= full step =================
+    {
+        float cl = 0.0f;
+        {
+            float v[CPL][5];
+#pragma unroll
+            for (int m = 0; m < CPL; ++m) {
+                float cs, p;
+                cell_flux<M>(u1[m], bc[m], v[m], cs, p);
+                if (tm.valid[m]) {
+                    cl = fmaxf(cl, cs);
+                    if (!(p > 0.0f)) bad |= MHD_HEALTH_PRESSURE;
+                }
+            }
+            const float c = tm.pencil_max(cl, rq);
+            cl = c;
+            const bool cpos = c > 0.0f;
+            const float yc = cpos ? M::recip(c) : 0.0f;
+            // exchange fr = c(u1+v) in x[0:5n) and wl = u1-v in x[5n:10n)
+#pragma unroll
+            for (int m = 0; m < CPL; ++m)
+#pragma unroll
+                for (int ii = 0; ii < 5; ++ii) {
+                    const float vv = cpos ? M::divy(v[m][ii], c, yc) : v[m][ii];
+                    if (tm.valid[m]) {
+                        x[ii * n + tm.cell[m]] = M::mul(c, M::add(u1[m][ii], vv));
+                        x[(5 + ii) * n + tm.cell[m]] = M::sub(u1[m][ii], vv);
+                    }
+                }
+        }
+        const float c = cl;
+        tm.sync();
+        // flux = (fr - fl + dfr - dfl)/2 with van Leer slopes (tvd1.c:54-112);
+        // fl(i) = c wl(i+1), fl(i+1) = c wl(i+2), fl(i-1) = c wl(i).  The
+        // limiter inputs are the undivided differences (the reference's /2
+        // factors cancel exactly in 2ab/(a+b)).
+        float fx[CPL][5];
+#pragma unroll
+        for (int m = 0; m < CPL; ++m)
+#pragma unroll
+            for (int ii = 0; ii < 5; ++ii) {
+                const float f0 = x[ii * n + tm.cell[m]];
+                const float frp = x[ii * n + tm.ip[m]];
+                const float frm = x[ii * n + tm.im[m]];
+                const float dfr = M::slope(M::sub(frp, f0), M::sub(f0, frm));
+                const float fl0 = M::mul(c, x[(5 + ii) * n + tm.ip[m]]);
+                const float flp = M::mul(c, x[(5 + ii) * n + tm.ipp[m]]);
+                const float flm = M::mul(c, x[(5 + ii) * n + tm.cell[m]]);
+                const float dfl = M::slope(M::sub(fl0, flp), M::sub(flm, fl0));
+                fx[m][ii] = 0.5f * M::add(M::sub(f0, fl0), M::sub(dfr, dfl));
+            }
+        tm.sync();
+#pragma unroll
+        for (int m = 0; m < CPL; ++m)
+            if (tm.valid[m])
+#pragma unroll
+                for (int ii = 0; ii < 5; ++ii) x[ii * n + tm.cell[m]] = fx[m][ii];
+        tm.sync();
+        // u = u - (flux - cshift(flux,-1)) dt, written back into US
+        const float mdt = -dt;
+#pragma unroll
+        for (int m = 0; m < CPL; ++m) {
+            if (!(live && tm.valid[m])) continue;
+            const int cc = tm.cell[m];
+            float s = 0.0f, r = 0.0f;
+#pragma unroll
+            for (int ii = 0; ii < 5; ++ii) {
+                const float d = M::sub(fx[m][ii], x[ii * n + tm.im[m]]);
+                const float un = M::add(us[cc * 5 + ii], M::mul(mdt, d));
+                us[cc * 5 + ii] = un;
+                s += un;
+                if (ii == 0) r = un;
+            }
+            if (!(r > 0.0f)) bad |= MHD_HEALTH_DENSITY;
+            if (!isfinite(s)) bad |= MHD_HEALTH_NONFINITE;
+        }
+    }
+
+    if (!live) bad = 0;
+    if (bad) flag_health(a.health, bad);
+    __syncthreads();
+    if (!ROWS) {
+        block_copy_out(a.u_out + p0 * 5 * n, US, (long long)nvalid * 5 * n, threadIdx.x, blockDim.x);
+    } else {
+        const long long kb = (long long)k * f.sk;
+        const int ru = 5 * nvalid;
+        int off[2];
+        bool on[2];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int r = lane + 32 * h;
+            on[h] = r < ru;
+            const int qq = r / 5, p = r - qq * 5;
+            off[h] = qq * ps + nib(f.iu, p);
+        }
+        for (int i = warp; i < n; i += nwarps) {
+            float *g = a.u_out + (kb + (long long)i * f.si + j0) * 5;
+#pragma unroll
+            for (int h = 0; h < 2; ++h)
+                if (on[h]) g[lane + 32 * h] = US[off[h] + i * 5];
+        }
+    }
+}
+
+// Launch one instantiation; sets the dynamic shared-memory attribute once per
+// instantiation when above the 48 KB default.
+template <int CPL, int WPP, class M, bool ROWS>
+cudaError_t launch_fluidx_inst(const FluidxArgs &a, int ppc, cudaStream_t s)
+{
+    static size_t smem_set = 0;
+    const int threads = 32 * WPP * ppc;
+    const long long blocks = ROWS ? (long long)((a.f.ny + ppc - 1) / ppc) * a.f.nz
+                                  : (a.f.npen + ppc - 1) / ppc;
+    const size_t smem = sizeof(float) * (size_t)fx_smem_floats(a.f.n, ppc, WPP, ROWS);
+    if (smem > 227 * 1024) return cudaErrorInvalidConfiguration;
+    if (smem > 48 * 1024 && smem_set < smem) {
+        cudaError_t e = cudaFuncSetAttribute(fluidx_kernel<CPL, WPP, M, ROWS>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        smem_set = smem;
+    }
+    fluidx_kernel<CPL, WPP, M, ROWS><<<(unsigned)blocks, threads, smem, s>>>(a);
+    return cudaGetLastError();
+}
+
+// dispatch over the supported team shapes and both staging modes (rows mode
+// when the frame's pencils run across memory, sj == 1 and si != 1)
+template <class M>
+cudaError_t launch_fluidx_policy(const FluidxArgs &a, const PencilCfg &cfg, cudaStream_t s)
+{
+    const bool rows = a.f.si != 1;
+#define MHD_FX(C, W)                                                                  \
+    if (cfg.cpl == C && cfg.wpp == W)                                                 \
+        return rows ? launch_fluidx_inst<C, W, M, true>(a, cfg.ppc, s)                \
+                    : launch_fluidx_inst<C, W, M, false>(a, cfg.ppc, s);
+    MHD_PENCIL_SHAPES(MHD_FX)
+#undef MHD_FX
+    return cudaErrorInvalidConfiguration;
+}
+
+}  // namespace mhd

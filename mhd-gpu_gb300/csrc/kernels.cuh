@@ -30,10 +30,32 @@ struct AdvectArgs {
 // pencil, PPC pencils per CTA
 struct PencilCfg { int cpl, wpp, ppc; };
 
+// the (CPL, WPP) pairs that are compiled
+#define MHD_PENCIL_SHAPES(X) \
+    X(1, 1) X(2, 1) X(4, 1) X(1, 2) X(2, 2) X(4, 2) X(1, 4) X(2, 4) X(4, 4) X(2, 8) X(4, 8)
+
+inline bool pencil_shape_ok(const PencilCfg &c, int n)
+{
+    bool known = false;
+#define MHD_SHAPE_KNOWN(C, W) known = known || (c.cpl == C && c.wpp == W);
+    MHD_PENCIL_SHAPES(MHD_SHAPE_KNOWN)
+#undef MHD_SHAPE_KNOWN
+    return known && c.ppc >= 1 && 32 * c.wpp * c.ppc <= 256 && n <= 32 * c.wpp * c.cpl;
+}
+
 PencilCfg fluidx_pick(int n);
 PencilCfg advect_pick(int n);
-cudaError_t launch_fluidx(const FluidxArgs &a, const PencilCfg &cfg, cudaStream_t s);
-cudaError_t launch_advect(const AdvectArgs &a, const PencilCfg &cfg, cudaStream_t s);
+bool frame_supported(const Frame &f);
+// the shape in use for a kernel class, pencil length and staging mode (rows:
+// pencils across memory): the tuned one if the autotuner (or mhdgpu_set_tile)
+// recorded it, else the default table
+PencilCfg pencil_cfg(int kclass, int n, bool rows = false);
+PencilCfg rows_pick(int n);
+int math_mode();
+cudaError_t launch_fluidx(const FluidxArgs &a, const PencilCfg &cfg, int math, cudaStream_t s);
+cudaError_t launch_fluidx_faithful(const FluidxArgs &a, const PencilCfg &cfg, cudaStream_t s);
+cudaError_t launch_fluidx_fast(const FluidxArgs &a, const PencilCfg &cfg, cudaStream_t s);
+cudaError_t launch_advect(const AdvectArgs &a, const PencilCfg &cfg, int math, cudaStream_t s);
 cudaError_t launch_transpose(float *du, float *db, const float *su, const float *sb,
                              int nx, int ny, int nz, int which, cudaStream_t s);
 cudaError_t launch_cfl(const float *u, const float *b, int nx, int ny, int nz, int mode,

@@ -12,12 +12,18 @@
 
 namespace mhd {
 
-// Pencil geometry of one frame in the reference layout u(5,n,ny,nz),
-// b(3,n,ny,nz): the pencil runs along the fastest spatial axis (length n),
-// pencil index p = j + ny*k.
+// Pencil geometry of one frame: the frame's axes (i, j, k) have extents
+// (n, ny, nz) and cell strides (si, sj, sk) in the stored array, and frame
+// component f of u (of b) is stored component (pu >> 4f) & 15 ((pb >> 4f) & 15);
+// iu, ib are the inverse maps.  The reference layout u(5,n,ny,nz) seen as
+// itself is si = 1, sj = n, sk = n*ny with identity maps (make_frame); the
+// y and z sweeps of a box stored x-major are strided views of the same array
+// (make_view), which is how the transpose-free step avoids transposing.
 struct Frame {
     int n, ny, nz;
     long long npen;
+    long long si, sj, sk;
+    unsigned pu, pb, iu, ib;
 };
 
 __host__ __device__ inline Frame make_frame(int n, int ny, int nz)
@@ -25,8 +31,35 @@ __host__ __device__ inline Frame make_frame(int n, int ny, int nz)
     Frame f;
     f.n = n; f.ny = ny; f.nz = nz;
     f.npen = (long long)ny * (long long)nz;
+    f.si = 1; f.sj = n; f.sk = (long long)n * ny;
+    f.pu = 0x43210u; f.pb = 0x210u; f.iu = 0x43210u; f.ib = 0x210u;
     return f;
 }
+
+// Frames of the sweeps of an nx*ny*nz box stored x-major (axis 0, 1, 2 = x, y, z):
+//   x: (x, y, z), u (rho, m_x, m_y, m_z, E), b (b_x, b_y, b_z)
+//   y: (y, x, z), u (rho, m_y, m_x, m_z, E), b (b_y, b_x, b_z)   [after transpose12]
+//   z: (z, x, y), u (rho, m_z, m_x, m_y, E), b (b_z, b_x, b_y)   [after transpose12, 13]
+// (Heterogeneous_MHD/C/mhd.c:72-119 with transpose12.c / transpose13.c).
+__host__ __device__ inline Frame make_view(int axis, int nx, int ny, int nz)
+{
+    Frame f;
+    const long long sxy = (long long)nx * ny;
+    if (axis == 0) return make_frame(nx, ny, nz);
+    if (axis == 1) {
+        f.n = ny; f.ny = nx; f.nz = nz;
+        f.si = nx; f.sj = 1; f.sk = sxy;
+        f.pu = 0x43120u; f.pb = 0x201u; f.iu = 0x43120u; f.ib = 0x201u;
+    } else {
+        f.n = nz; f.ny = nx; f.nz = ny;
+        f.si = sxy; f.sj = 1; f.sk = nx;
+        f.pu = 0x42130u; f.pb = 0x102u; f.iu = 0x41320u; f.ib = 0x021u;
+    }
+    f.npen = (long long)f.ny * f.nz;
+    return f;
+}
+
+__host__ __device__ __forceinline__ int nib(unsigned m, int f) { return (int)((m >> (4 * f)) & 15u); }
 
 // A team of TPP = 32*WPP threads owns one pencil; thread t holds the CPL
 // cells c = m*TPP + t (m < CPL).  Cells >= n are padding: they compute on
@@ -90,22 +123,42 @@ __device__ __forceinline__ void flag_health(unsigned *health, unsigned bits)
     if (health) atomicOr(health, bits);
 }
 
+// Asynchronous 4-byte global -> shared copy (cp.async, no register round
+// trip): a thread can have all of its staging copies in flight at once.
+// Complete them with cp_async_wait_all() and then a barrier.
+__device__ __forceinline__ void cp_async4(float *smem_dst, const float *gmem_src)
+{
+    const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem_dst));
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem_src) : "memory");
+}
+
+__device__ __forceinline__ void cp_async16(void *smem_dst, const void *gmem_src)
+{
+    const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem_dst));
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem_src) : "memory");
+}
+
+__device__ __forceinline__ void cp_async_wait_all()
+{
+    asm volatile("cp.async.wait_all;\n" ::: "memory");
+}
+
 // Cooperative copy of `count` floats, 16-byte vectors when both ends allow it.
-// Plain (coherent) loads: the fluid kernels may run in place, so the source
-// is not read-only for the kernel's lifetime.
+// Coherent cp.async copies (the fluid kernels may run in place, so the
+// source is not read-only for the kernel's lifetime); every copy of the
+// calling thread is complete on return, the caller's barrier publishes them.
 __device__ __forceinline__ void block_copy_in(float *__restrict__ dst, const float *__restrict__ src,
                                               long long count, int tid, int nthreads)
 {
     const bool vec = ((reinterpret_cast<uintptr_t>(src) | reinterpret_cast<uintptr_t>(dst)) & 15u) == 0
                      && (count & 3) == 0;
     if (vec) {
-        const float4 *s4 = reinterpret_cast<const float4 *>(src);
-        float4 *d4 = reinterpret_cast<float4 *>(dst);
         const long long n4 = count >> 2;
-        for (long long i = tid; i < n4; i += nthreads) d4[i] = s4[i];
+        for (long long i = tid; i < n4; i += nthreads) cp_async16(dst + 4 * i, src + 4 * i);
     } else {
-        for (long long i = tid; i < count; i += nthreads) dst[i] = src[i];
+        for (long long i = tid; i < count; i += nthreads) cp_async4(dst + i, src + i);
     }
+    cp_async_wait_all();
 }
 
 __device__ __forceinline__ void block_copy_out(float *__restrict__ dst, const float *__restrict__ src,

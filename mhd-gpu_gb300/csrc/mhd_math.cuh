@@ -91,34 +91,128 @@ MHD_HD float add_sqrt(float x, float a)
     return fadd(sh, fadd(sl, zl));
 }
 
-// Fluxes v (already divided by nothing) and fast speed of one cell
+// ---------------------------------------------------------------------------
+// Approximate hardware reciprocal and reciprocal square root (MUFU).  They
+// only ever seed a correction step below, never produce a result on their own
+// in the faithful policy.
+// ---------------------------------------------------------------------------
+#if defined(__CUDA_ARCH__)
+MHD_HD float rcp_approx(float d)
+{
+    float y;
+    asm("rcp.approx.f32 %0, %1;" : "=f"(y) : "f"(d));
+    return y;
+}
+MHD_HD float rsqrt_approx(float a)
+{
+    float y;
+    asm("rsqrt.approx.f32 %0, %1;" : "=f"(y) : "f"(a));
+    return y;
+}
+MHD_HD float rcp_rn(float d) { return __frcp_rn(d); }
+#else
+MHD_HD float rcp_approx(float d) { return 1.0f / d; }
+MHD_HD float rsqrt_approx(float a) { return 1.0f / sqrtf(a); }
+MHD_HD float rcp_rn(float d) { volatile float r = 1.0f / d; return r; }
+#endif
+
+// Faithful policy: the rounding of the reference C path.
+//  - mul/add/sub round separately (no contraction);
+//  - a quotient a/d whose divisor is shared (1/rho of a cell, 1/c of a pencil)
+//    uses y = RN(1/d) once and Markstein's correction q = RN(q0 + (a - d q0) y),
+//    q0 = RN(a y) (P. Markstein, IBM J. Res. Dev. 34(1), 1990), which equals
+//    the IEEE quotient RN(a/d) for normal operands;
+//  - slope(X, Y) is the van Leer limiter 2ab/(a+b) of a = X/2, b = Y/2, i.e.
+//    XY/(X+Y), with the exact product XY as the reference's double numerator
+//    (Heterogeneous_MHD/C/tvd1.c:78, tvdb.c:75) and one correction step.
+struct Faithful {
+    MHD_HD static float mul(float a, float b) { return fmul(a, b); }
+    MHD_HD static float add(float a, float b) { return fadd(a, b); }
+    MHD_HD static float sub(float a, float b) { return fsub(a, b); }
+    MHD_HD static float recip(float d) { return rcp_rn(d); }
+    MHD_HD static float divy(float a, float d, float y)
+    {
+        const float q = fmul(a, y);
+        const float e = ffma(-q, d, a);
+        return ffma(e, y, q);
+    }
+    MHD_HD static float div(float a, float d) { return fdiv(a, d); }
+    // RN(2 v + s) formed once (the reference's double (s + 2.0*v)/4.0)
+    MHD_HD static float twice_plus(float v, float s) { return ffma(2.0f, v, s); }
+    // RN(b - p/2) formed once (the reference's double b - p/2.0)
+    MHD_HD static float minus_half(float b, float p) { return ffma(-0.5f, p, b); }
+    MHD_HD static float slope(float X, float Y)
+    {
+        const float ph = fmul(X, Y);
+        if (!(ph > 0.0f)) return 0.0f;
+        const float pl = ffma(X, Y, -ph);
+        const float s = fadd(X, Y);
+        const float y = rcp_approx(s);
+        const float q0 = fmul(ph, y);
+        const float e = fadd(ffma(-q0, s, ph), pl);
+        return ffma(e, y, q0);
+    }
+    MHD_HD static float pressure(float e, float q, float b2) { return total_pressure(e, q, b2); }
+    // RN(x + sqrt(a)) with the root in float-float: zh ~ sqrt(a) from the
+    // hardware rsqrt, zl = (a - zh^2)/(2 zh) with the exact FMA residual.
+    MHD_HD static float speed(float x, float a)
+    {
+        if (!(a > 0.0f)) return x;
+        const float r = rsqrt_approx(a);
+        const float zh = fmul(a, r);
+        const float zl = fmul(ffma(-zh, zh, a), 0.5f * r);
+        const float hi = fmaxf(x, zh), lo = fminf(x, zh);
+        const float sh = fadd(hi, lo);
+        const float sl = fsub(lo, fsub(sh, hi));          // Fast2Sum, |hi| >= |lo|
+        return fadd(sh, fadd(sl, zl));
+    }
+};
+
+// Fast policy: plain FP32 with FMA contraction allowed, hardware reciprocal
+// and root.  Measured against the oracle like the faithful policy.
+struct Fast {
+    MHD_HD static float mul(float a, float b) { return a * b; }
+    MHD_HD static float add(float a, float b) { return a + b; }
+    MHD_HD static float sub(float a, float b) { return a - b; }
+    MHD_HD static float recip(float d) { return rcp_approx(d); }
+    MHD_HD static float divy(float a, float d, float y) { (void)d; return a * y; }
+    MHD_HD static float div(float a, float d) { return a * rcp_approx(d); }
+    MHD_HD static float twice_plus(float v, float s) { return 2.0f * v + s; }
+    MHD_HD static float minus_half(float b, float p) { return b - 0.5f * p; }
+    MHD_HD static float slope(float X, float Y)
+    {
+        const float p = X * Y;
+        return (p > 0.0f) ? p * rcp_approx(X + Y) : 0.0f;
+    }
+    MHD_HD static float pressure(float e, float q, float b2)
+    {
+        return (e - 0.5f * q) * kGammaM1 + b2 * kTwoMGammaHalf;
+    }
+    MHD_HD static float speed(float x, float a) { return (a > 0.0f) ? x + a * rsqrt_approx(a) : x; }
+};
+
+// Fluxes v (not yet divided by the pencil's c) and fast speed of one cell
 // (Heterogeneous_MHD/C/mhdflux.c:9-59).  u = (rho, m1, m2, m3, E) of the
 // frame, bc = cell-centred B of the frame.  Returns the gas pressure in p.
+template <class M>
 MHD_HD void cell_flux(const float u[5], const float bc[3], float v[5], float &cs, float &p)
 {
     const float r = u[0], m1 = u[1], m2 = u[2], m3 = u[3], e = u[4];
     const float bx = bc[0], by = bc[1], bz = bc[2];
-    const float vx = fdiv(m1, r);
-    const float b2 = fadd(fadd(fmul(bx, bx), fmul(by, by)), fmul(bz, bz));
-    const float s2 = fadd(fadd(fmul(m1, m1), fmul(m2, m2)), fmul(m3, m3));
-    const float ps = total_pressure(e, fdiv(s2, r), b2);
+    const float yr = M::recip(r);
+    const float vx = M::divy(m1, r, yr);
+    const float b2 = M::add(M::add(M::mul(bx, bx), M::mul(by, by)), M::mul(bz, bz));
+    const float s2 = M::add(M::add(M::mul(m1, m1), M::mul(m2, m2)), M::mul(m3, m3));
+    const float ps = M::pressure(e, M::divy(s2, r, yr), b2);
     v[0] = m1;
-    v[1] = fsub(fadd(fmul(m1, vx), ps), fmul(bx, bx));
-    v[2] = fsub(fmul(m2, vx), fmul(by, bx));
-    v[3] = fsub(fmul(m3, vx), fmul(bz, bx));
-    const float dot = fadd(fadd(fmul(bx, m1), fmul(by, m2)), fmul(bz, m3));
-    v[4] = fsub(fmul(fadd(e, ps), vx), fdiv(fmul(bx, dot), r));
-    p = fsub(ps, 0.5f * b2);                               // mhdflux.c:39-42, one rounding
-    const float a = fdiv(fadd(b2, fmul(kGamma, p)), r);
-    cs = add_sqrt(fabsf(vx), fabsf(a));
-}
-
-// van Leer slope of two one-sided differences: 2ab/(a+b) if ab > 0 else 0
-// (Heterogeneous_MHD/C/tvd1.c:71-81).
-MHD_HD float van_leer(float a, float b)
-{
-    const float ab = fmul(a, b);
-    return (ab > 0.0f) ? fdiv(2.0f * ab, fadd(a, b)) : 0.0f;
+    v[1] = M::sub(M::add(M::mul(m1, vx), ps), M::mul(bx, bx));
+    v[2] = M::sub(M::mul(m2, vx), M::mul(by, bx));
+    v[3] = M::sub(M::mul(m3, vx), M::mul(bz, bx));
+    const float dot = M::add(M::add(M::mul(bx, m1), M::mul(by, m2)), M::mul(bz, m3));
+    v[4] = M::sub(M::mul(M::add(e, ps), vx), M::divy(M::mul(bx, dot), r, yr));
+    p = M::sub(ps, 0.5f * b2);                             // mhdflux.c:39-42, one rounding
+    const float a = M::divy(M::add(b2, M::mul(kGamma, p)), r, yr);
+    cs = M::speed(fabsf(vx), fabsf(a));
 }
 
 // Fast speed of one cell for the CFL condition, C-path formula with the

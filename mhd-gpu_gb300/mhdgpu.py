@@ -33,7 +33,9 @@ EXPORTS = [
     "mhdgpu_advectbyzx_noalloc",
     "mhdgpu_transpose12", "mhdgpu_transpose13", "mhdgpu_cfl", "mhdgpu_dt_update",
     "mhdgpu_copy_matrix", "mhdgpu_step_workspace_bytes", "mhdgpu_step", "mhdgpu_advance",
-    "mhdgpu_run_host", "mhdgpu_profiler_create", "mhdgpu_profiler_destroy",
+    "mhdgpu_step_fused_workspace_bytes", "mhdgpu_step_fused",
+    "mhdgpu_run_host", "mhdgpu_set_math", "mhdgpu_set_tile", "mhdgpu_get_tile",
+    "mhdgpu_autotune", "mhdgpu_profiler_create", "mhdgpu_profiler_destroy",
     "mhdgpu_profiler_attach", "mhdgpu_profiler_reset", "mhdgpu_profiler_summary",
     # include/mhdgpu_compat.h
     "fluidx", "advectbyzx", "transpose12", "transpose13", "calcfl", "copy_matrix",
@@ -79,8 +81,14 @@ def lib() -> C.CDLL:
             "mhdgpu_copy_matrix": (I, [P, P, P, P, I, I, I, P]),
             "mhdgpu_step_workspace_bytes": (S, [I, I, I]),
             "mhdgpu_step": (I, [P, P, I, I, I, P, P, P, P]),
-            "mhdgpu_advance": (I, [P, P, I, I, I, I, D, I, F, P, P, P, P]),
-            "mhdgpu_run_host": (I, [P, P, I, I, I, D, I, P, F, I, P, P]),
+            "mhdgpu_step_fused_workspace_bytes": (S, [I, I, I]),
+            "mhdgpu_step_fused": (I, [P, P, I, I, I, P, P, P, P]),
+            "mhdgpu_advance": (I, [P, P, I, I, I, I, D, I, F, P, P, P, I, P]),
+            "mhdgpu_run_host": (I, [P, P, I, I, I, D, I, P, F, I, P, P, I]),
+            "mhdgpu_set_math": (I, [I]),
+            "mhdgpu_set_tile": (I, [I, I, I, I, I]),
+            "mhdgpu_get_tile": (I, [I, I, P, P, P]),
+            "mhdgpu_autotune": (I, [I, I, I, I]),
             "mhdgpu_profiler_create": (I, [P, I]),
             "mhdgpu_profiler_destroy": (I, [P]),
             "mhdgpu_profiler_attach": (I, [P]),
@@ -144,7 +152,13 @@ def dt_update(d_inv_c, cfl_number, tf, d_t, d_dt, stream=None):
                                   _stream(stream)))
 
 
-def step_workspace_bytes(nx, ny, nz) -> int:
+MHD_PATH_PLAIN = 0
+MHD_PATH_FUSED = 1
+
+
+def step_workspace_bytes(nx, ny, nz, path=MHD_PATH_PLAIN) -> int:
+    if path == MHD_PATH_FUSED:
+        return int(lib().mhdgpu_step_fused_workspace_bytes(nx, ny, nz))
     return int(lib().mhdgpu_step_workspace_bytes(nx, ny, nz))
 
 
@@ -153,11 +167,17 @@ def step(u, b, nx, ny, nz, d_dt, work, health=None, stream=None):
                              _stream(stream)))
 
 
-def advance(u, b, nx, ny, nz, nsteps, cfl_number, cfl_mode, tf, clock, dt_log, work, stream=None):
+def step_fused(u, b, nx, ny, nz, d_dt, work, health=None, stream=None):
+    _check(lib().mhdgpu_step_fused(_p(u), _p(b), nx, ny, nz, _p(d_dt), _p(work), _p(health),
+                                   _stream(stream)))
+
+
+def advance(u, b, nx, ny, nz, nsteps, cfl_number, cfl_mode, tf, clock, dt_log, work,
+            path=MHD_PATH_PLAIN, stream=None):
     """clock: a torch uint8 CUDA tensor of sizeof(Clock) bytes (see new_clock)."""
     _check(lib().mhdgpu_advance(_p(u), _p(b), nx, ny, nz, int(nsteps), float(cfl_number),
                                 int(cfl_mode), float(tf), _p(clock), _p(dt_log), _p(work),
-                                _stream(stream)))
+                                int(path), _stream(stream)))
 
 
 def new_clock(device="cuda", t=0.0):
@@ -174,7 +194,7 @@ def read_clock(clock) -> Clock:
 
 
 def run_host(u, b, nx, ny, nz, cfl_number=0.9, cfl_mode=MHD_CFL_C, t=0.0, tf=0.0,
-             max_steps=1, dt_log=None):
+             max_steps=1, dt_log=None, path=MHD_PATH_PLAIN):
     """End-to-end call on host numpy arrays (float32, modified in place).
 
     Returns (status, t, steps_done); status MHD_ERR_UNPHYSICAL is returned, not
@@ -186,10 +206,50 @@ def run_host(u, b, nx, ny, nz, cfl_number=0.9, cfl_mode=MHD_CFL_C, t=0.0, tf=0.0
     log_ptr = None if dt_log is None else dt_log.ctypes.data_as(C.c_void_p)
     st = lib().mhdgpu_run_host(u.ctypes.data_as(C.c_void_p), b.ctypes.data_as(C.c_void_p), nx, ny,
                                nz, float(cfl_number), int(cfl_mode), C.byref(tt), float(tf),
-                               int(max_steps), log_ptr, C.byref(done))
+                               int(max_steps), log_ptr, C.byref(done), int(path))
     if st not in (MHD_OK, MHD_ERR_UNPHYSICAL):
         _check(st)
     return st, tt.value, done.value
+
+
+MHD_MATH_FAITHFUL = 0
+MHD_MATH_FAST = 1
+
+
+def set_math(mode: int) -> int:
+    """Select the arithmetic policy of the pencil kernels; returns the previous one."""
+    prev = lib().mhdgpu_set_math(int(mode))
+    if prev < 0:
+        raise MhdError(MHD_ERR_ARG, lib().mhdgpu_last_error().decode())
+    return prev
+
+
+MHD_TILE_ROWS = 16
+
+
+def set_tile(kclass: str, n: int, cpl: int, wpp: int, ppc: int, rows: bool = False):
+    """rows: the shape for pencils that run across memory (transpose-free y/z sweeps)."""
+    _check(lib().mhdgpu_set_tile(KCLASS[kclass] | (MHD_TILE_ROWS if rows else 0), n, cpl, wpp, ppc))
+
+
+def get_tile(kclass: str, n: int, rows: bool = False):
+    c, w, p = C.c_int(), C.c_int(), C.c_int()
+    _check(lib().mhdgpu_get_tile(KCLASS[kclass] | (MHD_TILE_ROWS if rows else 0), n,
+                                 C.byref(c), C.byref(w), C.byref(p)))
+    return c.value, w.value, p.value
+
+
+def autotune(nx: int, ny: int, nz: int, math: int = MHD_MATH_FAITHFUL):
+    """Time every compiled team shape for the pencil lengths of this box and
+    keep the fastest (mhdgpu_autotune); returns {(kclass, n, rows): shape}."""
+    _check(lib().mhdgpu_autotune(nx, ny, nz, int(math)))
+    out = {}
+    for k in ("fluidx", "advectbyzx"):
+        for n in sorted({nx, ny, nz}):
+            out[(k, n, False)] = get_tile(k, n)
+        for n in sorted({ny, nz}):
+            out[(k, n, True)] = get_tile(k, n, rows=True)
+    return out
 
 
 class Profiler:

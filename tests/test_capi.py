@@ -64,8 +64,10 @@ def test_bad_arguments_are_rejected_without_a_gpu(L):
     # bad CFL mode
     assert L.mhdgpu_cfl(fake, fake, 8, 8, 8, 7, fake, fake, None) == mhdgpu.MHD_ERR_ARG
     # negative step count, bad cfl number
-    assert L.mhdgpu_advance(fake, fake, 8, 8, 8, -1, 0.9, 0, 0.0, fake, None, fake, None) == mhdgpu.MHD_ERR_ARG
-    assert L.mhdgpu_advance(fake, fake, 8, 8, 8, 1, 0.0, 0, 0.0, fake, None, fake, None) == mhdgpu.MHD_ERR_ARG
+    assert L.mhdgpu_advance(fake, fake, 8, 8, 8, -1, 0.9, 0, 0.0, fake, None, fake, 0, None) == mhdgpu.MHD_ERR_ARG
+    assert L.mhdgpu_advance(fake, fake, 8, 8, 8, 1, 0.0, 0, 0.0, fake, None, fake, 0, None) == mhdgpu.MHD_ERR_ARG
+    assert L.mhdgpu_advance(fake, fake, 8, 8, 8, 1, 0.9, 0, 0.0, fake, None, fake, 5, None) == mhdgpu.MHD_ERR_ARG
+    assert L.mhdgpu_step_fused(fake, fake, 8, 2000, 8, fake, fake, None, None) == mhdgpu.MHD_ERR_ARG
     assert L.mhdgpu_dt_update(fake, -1.0, 0.0, fake, fake, None) == mhdgpu.MHD_ERR_ARG
 
 
@@ -78,7 +80,22 @@ def test_partial_overlap_rejected(L):
     assert st == mhdgpu.MHD_ERR_ARG
 
 
+def test_tile_and_math_settings_without_a_gpu(L):
+    import mhdgpu
+    c, w, p = C.c_int(), C.c_int(), C.c_int()
+    assert L.mhdgpu_get_tile(0, 128, C.byref(c), C.byref(w), C.byref(p)) == 0
+    assert c.value * w.value * 32 >= 128
+    assert L.mhdgpu_set_tile(0, 128, 3, 1, 1) == mhdgpu.MHD_ERR_ARG      # not compiled
+    assert L.mhdgpu_set_tile(0, 300, 4, 1, 1) == mhdgpu.MHD_ERR_ARG      # does not cover
+    assert L.mhdgpu_set_tile(0, 64, 2, 1, 16) == mhdgpu.MHD_ERR_ARG      # 512 threads
+    assert L.mhdgpu_set_tile(2, 64, 2, 1, 1) == mhdgpu.MHD_ERR_ARG       # not a pencil kernel
+    assert L.mhdgpu_set_math(7) == -1
+    assert L.mhdgpu_set_math(0) == 0
+    assert L.mhdgpu_autotune(0, 4, 4, 0) == mhdgpu.MHD_ERR_ARG
+
+
 def test_workspace_sizes(L):
     assert L.mhdgpu_step_workspace_bytes(32, 32, 32) == 40 * 32 ** 3
     assert L.mhdgpu_advectbyzx_scratch_bytes(16, 8, 4) == 8 * 16 * 8 * 4
     assert L.mhdgpu_step_workspace_bytes(0, 1, 1) == 0
+    assert L.mhdgpu_step_fused_workspace_bytes(32, 16, 8) == 8 * 32 * 16 * 8

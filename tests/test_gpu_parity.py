@@ -172,22 +172,43 @@ def test_step_matches_oracle(gpu, oracle_lib, dims):
     assert max(field_errors(gb, rb, 3)) < TOL, field_errors(gb, rb, 3)
 
 
-def _advance(gpu, u, b, nx, ny, nz, nsteps, cfl_number, mode=0, tf=0.0):
+def _advance(gpu, u, b, nx, ny, nz, nsteps, cfl_number, mode=0, tf=0.0, path=0):
     import torch
     du, db = dev(u), dev(b)
-    work = torch.empty(gpu.step_workspace_bytes(nx, ny, nz), dtype=torch.uint8, device="cuda")
+    work = torch.empty(gpu.step_workspace_bytes(nx, ny, nz, path), dtype=torch.uint8, device="cuda")
     clock = gpu.new_clock()
     log = torch.zeros(max(nsteps, 1), dtype=torch.float32, device="cuda")
-    gpu.advance(du, db, nx, ny, nz, nsteps, cfl_number, mode, tf, clock, log, work)
+    gpu.advance(du, db, nx, ny, nz, nsteps, cfl_number, mode, tf, clock, log, work, path)
     clk = gpu.read_clock(clock)
     return host(du), host(db), host(log)[:clk.iter], clk
 
 
-def test_shipped_alfven_state_full_run_matches_reference(gpu):
+PATHS = [0, 1]   # MHD_PATH_PLAIN, MHD_PATH_FUSED
+
+
+@pytest.mark.parametrize("dims", [(16, 16, 16), (12, 10, 8), (32, 16, 24), (5, 7, 9), (64, 40, 24)])
+def test_fused_step_equals_plain_step_bitwise(gpu, dims):
+    """The transpose-free step does the same arithmetic per pencil as the
+    transposing one: equal bit for bit, on cubic and non-cubic boxes."""
+    import ics
+    import torch
+    nx, ny, nz = dims
+    u, b = ics.random_state(nx, ny, nz, seed=23, amp=0.2)
+    out = []
+    for path in PATHS:
+        du, db = dev(u), dev(b)
+        work = torch.empty(gpu.step_workspace_bytes(nx, ny, nz, path), dtype=torch.uint8, device="cuda")
+        (gpu.step if path == 0 else gpu.step_fused)(du, db, nx, ny, nz, scalar(0.05), work)
+        out.append((host(du), host(db)))
+    assert bits_equal(out[0][0], out[1][0]) and bits_equal(out[0][1], out[1][1])
+
+
+@pytest.mark.parametrize("path", PATHS)
+def test_shipped_alfven_state_full_run_matches_reference(gpu, path):
     """The reference's own run from data/source_init_alfvenlinear_16cube.dat:
     54 steps to tf = 64 at CFL 0.9 (Heterogeneous_MHD/C/mhd.c:59-125)."""
     g = np.load(os.path.join(GOLD, "alfven16_dat.npz"))
-    gu, gb, dts, clk = _advance(gpu, g["u0"], g["b0"], 16, 16, 16, 60, 0.9, tf=64.0)
+    gu, gb, dts, clk = _advance(gpu, g["u0"], g["b0"], 16, 16, 16, 60, 0.9, tf=64.0, path=path)
     # this state has plasma beta ~1e-3: the FP32 pressure recovery touches 0
     # at round-off (the warning bit), nothing worse
     assert clk.iter == 54
@@ -198,7 +219,8 @@ def test_shipped_alfven_state_full_run_matches_reference(gpu):
     assert max(eu) < TOL and max(eb) < TOL, (eu, eb)
 
 
-def test_config1_alfven_x_32_100_steps(gpu, oracle_lib):
+@pytest.mark.parametrize("path", PATHS)
+def test_config1_alfven_x_32_100_steps(gpu, oracle_lib, path):
     """32^3 Alfven wave along x, A=1e-3, CFL 0.7, 100 steps."""
     import ics
     O = oracle_lib.oracle("f32")
@@ -206,7 +228,7 @@ def test_config1_alfven_x_32_100_steps(gpu, oracle_lib):
     u, b = ics.alfven_x(32)
     ru, rb = u.copy(), b.copy()
     s, t, rdts = O.run(ru, rb, 32, 32, 32, cfl_number=0.7, max_steps=100)
-    gu, gb, dts, clk = _advance(gpu, u, b, 32, 32, 32, 100, 0.7)
+    gu, gb, dts, clk = _advance(gpu, u, b, 32, 32, 32, 100, 0.7, path=path)
     oracle_lib.set_threads(1)
     assert clk.iter == 100 and clk.health == 0
     assert np.abs(dts / rdts - 1).max() < 1e-6
@@ -215,7 +237,8 @@ def test_config1_alfven_x_32_100_steps(gpu, oracle_lib):
     assert ics.div_b(gb, 32, 32, 32) < 1e-6
 
 
-def test_oblique_alfven_64_matches_oracle(gpu, oracle_lib):
+@pytest.mark.parametrize("path", PATHS)
+def test_oblique_alfven_64_matches_oracle(gpu, oracle_lib, path):
     """The diagonal wave of the 128^3 configuration, at 64^3 for 30 steps."""
     import ics
     O = oracle_lib.oracle("f32")
@@ -224,7 +247,7 @@ def test_oblique_alfven_64_matches_oracle(gpu, oracle_lib):
     u, b = ics.alfven_oblique(n)
     ru, rb = u.copy(), b.copy()
     O.run(ru, rb, n, n, n, cfl_number=0.7, max_steps=30)
-    gu, gb, dts, clk = _advance(gpu, u, b, n, n, n, 30, 0.7)
+    gu, gb, dts, clk = _advance(gpu, u, b, n, n, n, 30, 0.7, path=path)
     oracle_lib.set_threads(1)
     eu, eb = field_errors(gu, ru, 5), field_errors(gb, rb, 3)
     assert max(eu) < TOL and max(eb) < TOL, (eu, eb)
@@ -233,7 +256,8 @@ def test_oblique_alfven_64_matches_oracle(gpu, oracle_lib):
     assert ics.div_b(gb, n, n, n) < 2.0 * ics.div_b(rb, n, n, n) + 1e-6
 
 
-def test_config2_full_size_invariants(gpu):
+@pytest.mark.parametrize("path", PATHS)
+def test_config2_full_size_invariants(gpu, path):
     """128^3 diagonal Alfven wave, 200 steps: div B stays at round-off, mass and
     energy are conserved to FP32 round-off, the wave amplitude decays only by
     the scheme's diffusion."""
@@ -241,7 +265,7 @@ def test_config2_full_size_invariants(gpu):
     n = 128
     u, b = ics.alfven_oblique(n)
     tot0 = ics.totals(u, n, n, n)
-    gu, gb, dts, clk = _advance(gpu, u, b, n, n, n, 200, 0.7)
+    gu, gb, dts, clk = _advance(gpu, u, b, n, n, n, 200, 0.7, path=path)
     assert clk.iter == 200 and clk.health == 0
     assert ics.div_b(gb, n, n, n) < 1e-5
     tot = ics.totals(gu, n, n, n)
@@ -252,13 +276,14 @@ def test_config2_full_size_invariants(gpu):
     assert 0.5 * amp0 < amp <= 1.01 * amp0
 
 
-def test_run_host_matches_device_path(gpu):
+@pytest.mark.parametrize("path", PATHS)
+def test_run_host_matches_device_path(gpu, path):
     import ics
     u, b = ics.alfven_x(16)
-    gu, gb, dts, clk = _advance(gpu, u, b, 16, 16, 16, 5, 0.7)
+    gu, gb, dts, clk = _advance(gpu, u, b, 16, 16, 16, 5, 0.7, path=path)
     hu, hb = u.copy(), b.copy()
     log = np.zeros(5, np.float32)
-    st, t, done = gpu.run_host(hu, hb, 16, 16, 16, 0.7, 0, 0.0, 0.0, 5, log)
+    st, t, done = gpu.run_host(hu, hb, 16, 16, 16, 0.7, 0, 0.0, 0.0, 5, log, path=path)
     assert st == gpu.MHD_OK and done == 5
     assert bits_equal(hu, gu) and bits_equal(hb, gb) and bits_equal(log, dts)
 
@@ -316,3 +341,126 @@ def test_compat_shims_match_oracle(gpu, oracle_lib):
     assert bits_equal(tu, su) and bits_equal(tb, sb)
     inv = L.calcfl(fp(u), fp(b), ip(nx), ip(ny), ip(nz))
     assert _ulps(inv, O.calcfl(u, b, nx, ny, nz)) <= 2
+
+
+SHAPES_COMPILED = [(1, 1), (2, 1), (4, 1), (1, 2), (2, 2), (4, 2), (1, 4), (2, 4), (4, 4), (2, 8), (4, 8)]
+
+
+@pytest.mark.parametrize("n", [16, 48, 100, 128, 256, 512])
+def test_every_team_shape_matches_oracle(gpu, oracle_lib, n):
+    """fluidx and advectbyzx under every compiled team shape that covers the
+    pencil (the shapes the autotuner chooses from)."""
+    import ics
+    import torch
+    O = oracle_lib.oracle("f32")
+    ny, nz = 3, 2
+    u, b = ics.random_state(n, ny, nz, seed=n)
+    dt = np.float32(0.03)
+    ref_u = np.zeros_like(u)
+    O.fluidx(ref_u, b.copy(), n, ny, nz, dt, u.copy(), b.copy())
+    ref_b = b.copy()
+    O.advectbyzx(u.copy(), ref_b, n, ny, nz, dt, u.copy(), b.copy())
+    saved = {k: gpu.get_tile(k, n) for k in ("fluidx", "advectbyzx")}
+    scr = torch.empty(gpu.advectbyzx_scratch_bytes(n, ny, nz) // 4, dtype=torch.float32, device="cuda")
+    tested = 0
+    try:
+        for cpl, wpp in SHAPES_COMPILED:
+            if n > 32 * wpp * cpl:
+                continue
+            for ppc in (1, 2, 4, 8):
+                if 32 * wpp * ppc > 256:
+                    continue
+                gpu.set_tile("fluidx", n, cpl, wpp, ppc)
+                gpu.set_tile("advectbyzx", n, cpl, wpp, ppc)
+                du, db = dev(u), dev(b)
+                out = dev(np.zeros_like(u))
+                gpu.fluidx(out, du, db, n, ny, nz, scalar(dt))
+                gpu.advectbyzx(db, du, n, ny, nz, scalar(dt), scr)
+                eu = field_errors(host(out), ref_u, 5)
+                eb = field_errors(host(db), ref_b, 3)
+                assert max(eu) < TOL and max(eb) < TOL, ((cpl, wpp, ppc), eu, eb)
+                tested += 1
+    finally:
+        for k, (c, w, p) in saved.items():
+            gpu.set_tile(k, n, c, w, p)
+    assert tested > 0
+
+
+@pytest.mark.parametrize("n", [16, 48, 100])
+def test_every_team_shape_fused_step_bitwise(gpu, n):
+    """The transpose-free step stages pencils that run across memory through
+    shared memory in rows; every compiled team shape must give the plain
+    step's bits."""
+    import ics
+    import torch
+    u, b = ics.random_state(n, n, n, seed=n + 1, amp=0.2)
+    du, db = dev(u), dev(b)
+    work = torch.empty(gpu.step_workspace_bytes(n, n, n), dtype=torch.uint8, device="cuda")
+    gpu.step(du, db, n, n, n, scalar(0.04), work)
+    ref_u, ref_b = host(du), host(db)
+    saved = {(k, r): gpu.get_tile(k, n, rows=r) for k in ("fluidx", "advectbyzx") for r in (False, True)}
+    wf = torch.empty(gpu.step_workspace_bytes(n, n, n, 1), dtype=torch.uint8, device="cuda")
+    try:
+        for cpl, wpp in SHAPES_COMPILED:
+            if n > 32 * wpp * cpl:
+                continue
+            for ppc in (1, 2, 4, 8):
+                if 32 * wpp * ppc > 256:
+                    continue
+                for k in ("fluidx", "advectbyzx"):
+                    for r in (False, True):
+                        gpu.set_tile(k, n, cpl, wpp, ppc, rows=r)
+                du, db = dev(u), dev(b)
+                gpu.step_fused(du, db, n, n, n, scalar(0.04), wf)
+                assert bits_equal(host(du), ref_u) and bits_equal(host(db), ref_b), (cpl, wpp, ppc)
+    finally:
+        for (k, r), (c, w, p) in saved.items():
+            gpu.set_tile(k, n, c, w, p, rows=r)
+
+
+def test_fast_math_policy_matches_oracle(gpu, oracle_lib):
+    """The fast policy (FMA contraction, hardware reciprocal and root): one
+    fluidx and one advectbyzx within the same 1e-5 tolerance."""
+    import ics
+    import torch
+    O = oracle_lib.oracle("f32")
+    nx, ny, nz = 64, 8, 6
+    u, b = ics.random_state(nx, ny, nz, seed=77)
+    dt = np.float32(0.03)
+    ref_u = np.zeros_like(u)
+    O.fluidx(ref_u, b.copy(), nx, ny, nz, dt, u.copy(), b.copy())
+    ref_b = b.copy()
+    O.advectbyzx(u.copy(), ref_b, nx, ny, nz, dt, u.copy(), b.copy())
+    prev = gpu.set_math(gpu.MHD_MATH_FAST)
+    try:
+        du, db = dev(u), dev(b)
+        scr = torch.empty(gpu.advectbyzx_scratch_bytes(nx, ny, nz) // 4, dtype=torch.float32, device="cuda")
+        gpu.fluidx(du, du, db, nx, ny, nz, scalar(dt))
+        gpu.advectbyzx(db, dev(u), nx, ny, nz, scalar(dt), scr)
+        assert max(field_errors(host(du), ref_u, 5)) < TOL
+        assert max(field_errors(host(db), ref_b, 3)) < TOL
+    finally:
+        gpu.set_math(prev)
+
+
+def test_autotune_keeps_parity(gpu, oracle_lib):
+    import ics
+    O = oracle_lib.oracle("f32")
+    nx, ny, nz = 48, 32, 20
+    saved = {(k, n, r): gpu.get_tile(k, n, rows=r) for k in ("fluidx", "advectbyzx")
+             for n in (nx, ny, nz) for r in (False, True)}
+    try:
+        picks = gpu.autotune(nx, ny, nz)
+        for (k, n, r), (c, w, p) in picks.items():
+            assert n <= 32 * w * c and 32 * w * p <= 256
+        u, b = ics.random_state(nx, ny, nz, seed=5, amp=0.2)
+        gu, gb, ru, rb, health = _step_parity(gpu, O, u, b, nx, ny, nz, np.float32(0.05))
+        assert max(field_errors(gu, ru, 5)) < TOL and max(field_errors(gb, rb, 3)) < TOL
+        import torch
+        du, db = dev(u), dev(b)
+        wf = torch.empty(gpu.step_workspace_bytes(nx, ny, nz, 1), dtype=torch.uint8, device="cuda")
+        gpu.step_fused(du, db, nx, ny, nz, scalar(0.05), wf)
+        assert bits_equal(host(du), gu) and bits_equal(host(db), gb)
+    finally:
+        for (k, n, r), (c, w, p) in saved.items():
+            gpu.set_tile(k, n, c, w, p, rows=r)
