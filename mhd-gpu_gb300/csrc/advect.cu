@@ -30,21 +30,24 @@ namespace mhd {
 __host__ __device__ inline int ax_r2(int ppc) { return 2 * (ppc + 1) + 1; }   // U2 row
 __host__ __device__ inline int ax_rk(int ppc) { return 2 * ppc + 1; }         // UK, BO row
 __host__ __device__ inline int ax_ro(int ppc) { return 4 * ppc + 1; }         // output row
+// exchange area of one pencil: 8 halo rows of n+3 floats (two alternating
+// groups of four)
+__host__ __device__ inline long long ax_xpen(int n) { return 8LL * (n + 3); }
 __host__ __device__ inline long long ax_smem_floats(int n, int ppc, bool rows)
 {
-    long long s = 8LL * n * ppc;
+    long long s = ax_xpen(n) * ppc;
     if (rows) s += (long long)n * (ax_r2(ppc) + 2 * ax_rk(ppc));
     return s;
 }
 
-template <int CPL, int WPP, class M, bool ROWS>
+template <int CPL, int WPP, class M, bool ROWS, int NT>
 __global__ void __launch_bounds__(256)
 advect_flux_kernel(AdvectArgs a)
 {
     constexpr int TPP = 32 * WPP;
     extern __shared__ float smem[];
     const Frame &f = a.f;
-    const int n = f.n;
+    const int n = NT > 0 ? NT : f.n;
     const int ppc = blockDim.x / TPP;
     const int q = threadIdx.x / TPP;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
@@ -60,13 +63,14 @@ advect_flux_kernel(AdvectArgs a)
         nvalid = min(ppc, f.ny - j0);
     }
     const bool live = ROWS ? q < nvalid : pen < f.npen;
-    float *xa = smem + (size_t)q * 8 * n;  // buffer 0
-    float *xb = xa + 4 * n;                // buffer 1
-    float *ST = smem + (size_t)ppc * 8 * n;
+    float *ST = smem + (size_t)ppc * ax_xpen(n);
 
-    Team<CPL, WPP> tm;
+    Team<CPL, WPP, NT> tm;
     tm.init(threadIdx.x - q * TPP, n);
     const float dt = *a.dt;
+    const int rs = tm.rs();
+    float *xbase = smem + (size_t)q * ax_xpen(n) + 1;
+    auto X = [&](int r) { return xbase + r * rs; };
 
     float vA[CPL], vB[CPL], bA[CPL], bB[CPL];
     long long base = 0;   // !ROWS: first stored cell of the pencil
@@ -81,8 +85,8 @@ advect_flux_kernel(AdvectArgs a)
         // vx = (m_x(jm) + m_x) / (rho(jm) + rho)  (A1.c:58, B1.c:51)
 #pragma unroll
         for (int m = 0; m < CPL; ++m) {
-            const int c = tm.cell[m];
-            if (live && tm.valid[m]) {
+            const int c = tm.ci(m);
+            if (live && tm.valid(m)) {
                 const float r0 = a.u[(base + c) * 5 + 0], m0 = a.u[(base + c) * 5 + 1];
                 const float rj = a.u[(bjm + c) * 5 + 0], mj = a.u[(bjm + c) * 5 + 1];
                 const float rk = a.u[(bkm + c) * 5 + 0], mk = a.u[(bkm + c) * 5 + 1];
@@ -97,7 +101,7 @@ advect_flux_kernel(AdvectArgs a)
     } else {
         // rows of the tile: U2 = (rho, m) of columns j0-1 .. j0+nvalid-1 at k,
         // UK = (rho, m) of columns j0 .. at k-1, BO = own (b(2), b(3))
-        float *U2 = ST;                                   // (ppc+1) * 2n
+        float *U2 = ST;
         const int r2 = ax_r2(ppc), rk = ax_rk(ppc);
         float *UK = U2 + (size_t)n * r2;                  // n * rk
         float *BO = UK + (size_t)n * rk;                  // n * rk
@@ -126,8 +130,8 @@ advect_flux_kernel(AdvectArgs a)
         __syncthreads();
 #pragma unroll
         for (int m = 0; m < CPL; ++m) {
-            const int c = tm.cell[m];
-            if (live && tm.valid[m]) {
+            const int c = tm.ci(m);
+            if (live && tm.valid(m)) {
                 const float *uo = U2 + c * r2 + 2 * (q + 1), *uj = U2 + c * r2 + 2 * q;
                 const float *uk = UK + c * rk + 2 * q, *bo = BO + c * rk + 2 * q;
                 vA[m] = M::div(M::add(uj[1], uo[1]), M::add(uj[0], uo[0]));
@@ -139,89 +143,88 @@ advect_flux_kernel(AdvectArgs a)
             }
         }
     }
+    // rows 0,1 <- the face velocities
 #pragma unroll
-    for (int m = 0; m < CPL; ++m)
-        if (tm.valid[m]) { xa[tm.cell[m]] = vA[m]; xa[n + tm.cell[m]] = vB[m]; }
+    for (int m = 0; m < CPL; ++m) { tm.put(X(0), m, vA[m]); tm.put(X(1), m, vB[m]); }
     tm.sync();
     // vx = (cshift(vx,-1) + cshift(vx,1) + 2 vx)/4: the (s + 2vx)/4 is formed
     // in double by the reference and rounded once; the quarter is exact.
+    // rows 4-7 <- vg and b*vg of both stages
     float gA[CPL], gB[CPL];   // smoothed velocities vg
 #pragma unroll
     for (int m = 0; m < CPL; ++m) {
-        const float sa = M::add(xa[tm.im[m]], xa[tm.ip[m]]);
-        const float sb = M::add(xa[n + tm.im[m]], xa[n + tm.ip[m]]);
+        const int c = tm.ci(m);
+        const float sa = M::add(X(0)[c - 1], X(0)[c + 1]);
+        const float sb = M::add(X(1)[c - 1], X(1)[c + 1]);
         gA[m] = 0.25f * M::twice_plus(vA[m], sa);
         gB[m] = 0.25f * M::twice_plus(vB[m], sb);
-        if (tm.valid[m]) {
-            const int c = tm.cell[m];
-            xb[c] = gA[m]; xb[n + c] = gB[m];
-            xb[2 * n + c] = M::mul(bA[m], gA[m]);
-            xb[3 * n + c] = M::mul(bB[m], gB[m]);
-        }
+        tm.put(X(4), m, gA[m]);
+        tm.put(X(5), m, gB[m]);
+        tm.put(X(6), m, M::mul(bA[m], gA[m]));
+        tm.put(X(7), m, M::mul(bB[m], gB[m]));
     }
     tm.sync();
-    // tvdb: vh = (vg + cshift(vg,1))/2 ; flux1 = b vg, upwinded by vh
+    // tvdb: vh = (vg + cshift(vg,1))/2 ; flux1 = b vg, upwinded by vh ; rows 0,1 <- flux1
     float hA[CPL], hB[CPL], f1A[CPL], f1B[CPL];
 #pragma unroll
     for (int m = 0; m < CPL; ++m) {
-        const int c = tm.cell[m], cp = tm.ip[m];
-        hA[m] = M::add(0.5f * gA[m], 0.5f * xb[cp]);
-        hB[m] = M::add(0.5f * gB[m], 0.5f * xb[n + cp]);
-        f1A[m] = (hA[m] > 0.0f) ? xb[2 * n + c] : xb[2 * n + cp];
-        f1B[m] = (hB[m] > 0.0f) ? xb[3 * n + c] : xb[3 * n + cp];
-        if (tm.valid[m]) { xa[c] = f1A[m]; xa[n + c] = f1B[m]; }
+        const int c = tm.ci(m);
+        hA[m] = M::add(0.5f * gA[m], 0.5f * X(4)[c + 1]);
+        hB[m] = M::add(0.5f * gB[m], 0.5f * X(5)[c + 1]);
+        f1A[m] = (hA[m] > 0.0f) ? X(6)[c] : X(6)[c + 1];
+        f1B[m] = (hB[m] > 0.0f) ? X(7)[c] : X(7)[c + 1];
+        tm.put(X(0), m, f1A[m]);
+        tm.put(X(1), m, f1B[m]);
     }
     tm.sync();
     // b1 = b - (flux1 - cshift(flux1,-1)) dt/2 : the product is float, the
     // halving and the subtraction double in the reference -> one rounding.
-    // Then exchange the products vg*b1.
+    // rows 4,5 <- vg*b1
 #pragma unroll
     for (int m = 0; m < CPL; ++m) {
-        const int cm = tm.im[m];
-        const float b1A = M::minus_half(bA[m], M::mul(M::sub(f1A[m], xa[cm]), dt));
-        const float b1B = M::minus_half(bB[m], M::mul(M::sub(f1B[m], xa[n + cm]), dt));
-        if (tm.valid[m]) {
-            const int c = tm.cell[m];
-            xb[c] = M::mul(gA[m], b1A);
-            xb[n + c] = M::mul(gB[m], b1B);
-        }
+        const int c = tm.ci(m);
+        const float b1A = M::minus_half(bA[m], M::mul(M::sub(f1A[m], X(0)[c - 1]), dt));
+        const float b1B = M::minus_half(bB[m], M::mul(M::sub(f1B[m], X(1)[c - 1]), dt));
+        tm.put(X(4), m, M::mul(gA[m], b1A));
+        tm.put(X(5), m, M::mul(gB[m], b1B));
     }
     tm.sync();
     // upwind second-order flux on the right face with the van Leer limiter;
     // wp, wm are half differences, so the slope of the undivided ones is
-    // 2 wm wp/(wm+wp) exactly (tvdb.c:64-75)
+    // 2 wm wp/(wm+wp) exactly (tvdb.c:64-75) ; rows 2,3 <- flux
     float flA[CPL], flB[CPL];
 #pragma unroll
     for (int m = 0; m < CPL; ++m) {
-        const int c = tm.cell[m], cp = tm.ip[m], cpp = tm.ipp[m], cm = tm.im[m];
+        const int c = tm.ci(m);
 #pragma unroll
         for (int s = 0; s < 2; ++s) {
-            const float *g = xb + s * n;
+            const float *g = X(4 + s) + c;
             const float h = s ? hB[m] : hA[m];
             float w, Wp, Wm;
             if (h > 0.0f) {
-                w = g[c];
-                Wp = M::sub(g[cp], w);
-                Wm = M::sub(w, g[cm]);
+                w = g[0];
+                Wp = M::sub(g[1], w);
+                Wm = M::sub(w, g[-1]);
             } else {
-                w = g[cp];
-                Wp = M::sub(w, g[cpp]);
-                Wm = M::sub(g[c], w);
+                w = g[1];
+                Wp = M::sub(w, g[2]);
+                Wm = M::sub(g[0], w);
             }
             const float dw = M::slope(Wm, Wp);
             const float fl = M::mul(M::add(w, dw), dt);
             if (s) flB[m] = fl; else flA[m] = fl;
         }
-        if (tm.valid[m]) { xa[2 * n + c] = flA[m]; xa[3 * n + c] = flB[m]; }
+        tm.put(X(2), m, flA[m]);
+        tm.put(X(3), m, flB[m]);
     }
     tm.sync();
     // b = b - (flux - cshift(flux,-1)) ; outputs b(2), b(3), sA, sB
     if (!ROWS) {
 #pragma unroll
         for (int m = 0; m < CPL; ++m) {
-            if (live && tm.valid[m]) {
-                const int c = tm.cell[m], cm = tm.im[m];
-                const float sa = xa[2 * n + cm], sb = xa[3 * n + cm];
+            if (live && tm.valid(m)) {
+                const int c = tm.ci(m);
+                const float sa = X(2)[c - 1], sb = X(3)[c - 1];
                 a.b[(base + c) * 3 + 1] = M::sub(bA[m], M::sub(flA[m], sa));
                 a.b[(base + c) * 3 + 2] = M::sub(bB[m], M::sub(flB[m], sb));
                 a.sA[base + c] = sa;
@@ -232,8 +235,8 @@ advect_flux_kernel(AdvectArgs a)
         float o[CPL][4];
 #pragma unroll
         for (int m = 0; m < CPL; ++m) {
-            const int cm = tm.im[m];
-            const float sa = xa[2 * n + cm], sb = xa[3 * n + cm];
+            const int c = tm.ci(m);
+            const float sa = X(2)[c - 1], sb = X(3)[c - 1];
             o[m][0] = M::sub(bA[m], M::sub(flA[m], sa));
             o[m][1] = M::sub(bB[m], M::sub(flB[m], sb));
             o[m][2] = sa;
@@ -244,9 +247,9 @@ advect_flux_kernel(AdvectArgs a)
         __syncthreads();   // the row staging is consumed
 #pragma unroll
         for (int m = 0; m < CPL; ++m)
-            if (live && tm.valid[m])
+            if (live && tm.valid(m))
 #pragma unroll
-                for (int w = 0; w < 4; ++w) OUT[tm.cell[m] * ro + 4 * q + w] = o[m][w];
+                for (int w = 0; w < 4; ++w) OUT[tm.ci(m) * ro + 4 * q + w] = o[m][w];
         __syncthreads();
         const long long kb = (long long)k * f.sk;
         const int p2 = nib(f.pb, 1), p3 = nib(f.pb, 2);
@@ -296,7 +299,7 @@ PencilCfg advect_pick(int n)
     return {4, 8, 1};
 }
 
-template <int CPL, int WPP, class M, bool ROWS>
+template <int CPL, int WPP, class M, bool ROWS, int NT>
 static cudaError_t launch_advect_inst(const AdvectArgs &a, int ppc, cudaStream_t s)
 {
     static size_t smem_set = 0;
@@ -306,23 +309,32 @@ static cudaError_t launch_advect_inst(const AdvectArgs &a, int ppc, cudaStream_t
     const size_t smem = sizeof(float) * (size_t)ax_smem_floats(a.f.n, ppc, ROWS);
     if (smem > 227 * 1024) return cudaErrorInvalidConfiguration;
     if (smem > 48 * 1024 && smem_set < smem) {
-        cudaError_t e = cudaFuncSetAttribute(advect_flux_kernel<CPL, WPP, M, ROWS>,
+        cudaError_t e = cudaFuncSetAttribute(advect_flux_kernel<CPL, WPP, M, ROWS, NT>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         smem_set = smem;
     }
-    advect_flux_kernel<CPL, WPP, M, ROWS><<<(unsigned)blocks, threads, smem, s>>>(a);
+    advect_flux_kernel<CPL, WPP, M, ROWS, NT><<<(unsigned)blocks, threads, smem, s>>>(a);
     return cudaGetLastError();
+}
+
+template <int C, int W, class M>
+static cudaError_t launch_advect_shape(const AdvectArgs &a, int ppc, bool rows, cudaStream_t s)
+{
+    constexpr int CAP = 32 * W * C;
+    if (a.f.n == CAP)
+        return rows ? launch_advect_inst<C, W, M, true, CAP>(a, ppc, s)
+                    : launch_advect_inst<C, W, M, false, CAP>(a, ppc, s);
+    return rows ? launch_advect_inst<C, W, M, true, 0>(a, ppc, s)
+                : launch_advect_inst<C, W, M, false, 0>(a, ppc, s);
 }
 
 template <class M>
 static cudaError_t launch_advect_policy(const AdvectArgs &a, const PencilCfg &cfg, cudaStream_t s)
 {
     const bool rows = a.f.si != 1;
-#define MHD_AX(C, W)                                                                  \
-    if (cfg.cpl == C && cfg.wpp == W)                                                 \
-        return rows ? launch_advect_inst<C, W, M, true>(a, cfg.ppc, s)                \
-                    : launch_advect_inst<C, W, M, false>(a, cfg.ppc, s);
+#define MHD_AX(C, W) \
+    if (cfg.cpl == C && cfg.wpp == W) return launch_advect_shape<C, W, M>(a, cfg.ppc, rows, s);
     MHD_PENCIL_SHAPES(MHD_AX)
 #undef MHD_AX
     return cudaErrorInvalidConfiguration;

@@ -15,8 +15,8 @@
 #include <string.h>
 #include <vector>
 
-#include "../../include/mhdgpu.h"
-#include "../../include/mhdgpu_compat.h"
+#include "mhdgpu.h"
+#include "mhdgpu_compat.h"
 
 namespace {
 

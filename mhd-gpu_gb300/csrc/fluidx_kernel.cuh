@@ -36,9 +36,11 @@ __host__ __device__ inline int fx_ps(int n, bool rows)          // u stride per 
     return rows ? 5 * n + ((37 - (5 * n) % 32) % 32) : 5 * n;   // = 5 (mod 32) for rows
 }
 __host__ __device__ inline int fx_bs(int n) { return 3 * n + ((35 - (3 * n) % 32) % 32); }
+// exchange area of one pencil: 10 halo rows of n+3 floats
+__host__ __device__ inline long long fx_xpen(int n) { return 10LL * (n + 3); }
 __host__ __device__ inline long long fx_xsize(int n, int ppc, bool rows)
 {
-    long long x = 10LL * n * ppc;
+    long long x = fx_xpen(n) * ppc;
     if (rows) {
         const long long need = (long long)(ppc + 1) * fx_bs(n) + (long long)(ppc + 1) * n;
         if (need > x) x = need;
@@ -50,14 +52,14 @@ __host__ __device__ inline long long fx_smem_floats(int n, int ppc, int wpp, boo
     return (long long)ppc * fx_ps(n, rows) + fx_xsize(n, ppc, rows) + (long long)ppc * wpp;
 }
 
-template <int CPL, int WPP, class M, bool ROWS>
+template <int CPL, int WPP, class M, bool ROWS, int NT>
 __global__ void __launch_bounds__(256)
 fluidx_kernel(FluidxArgs a)
 {
     constexpr int TPP = 32 * WPP;
     extern __shared__ float smem[];
     const Frame &f = a.f;
-    const int n = f.n;
+    const int n = NT > 0 ? NT : f.n;
     const int ppc = blockDim.x / TPP;
     const int q = threadIdx.x / TPP;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
@@ -84,12 +86,15 @@ fluidx_kernel(FluidxArgs a)
     float *XA = smem + (size_t)ppc * ps;                    // fx_xsize
     float *red = XA + fx_xsize(n, ppc, ROWS);               // ppc * WPP
     float *us = US + (size_t)q * ps;
-    float *x = XA + (size_t)q * 10 * n;
     float *rq = red + q * WPP;
 
-    Team<CPL, WPP> tm;
+    Team<CPL, WPP, NT> tm;
     tm.init(threadIdx.x - q * TPP, n);
     const float dt = *a.dt;
+    // exchange rows of this pencil: X(r)[c] for c in -1 .. n+1
+    const int rs = tm.rs();
+    float *x = XA + (size_t)q * fx_xpen(n) + 1;
+    auto X = [&](int r) { return x + r * rs; };
 
     // ---- stage u (kept) and b (transient) ----
     float bc[CPL][3];
@@ -106,9 +111,10 @@ fluidx_kernel(FluidxArgs a)
         const float *pb = XA + (size_t)q * 3 * n;
 #pragma unroll
         for (int m = 0; m < CPL; ++m) {
-            const int c = tm.cell[m];
-            if (live && tm.valid[m]) {
-                bc[m][0] = fadd(0.5f * pb[c * 3 + 0], 0.5f * pb[tm.ip[m] * 3 + 0]);
+            const int c = tm.ci(m);
+            const int cp = (c + 1 == n) ? 0 : c + 1;
+            if (live && tm.valid(m)) {
+                bc[m][0] = fadd(0.5f * pb[c * 3 + 0], 0.5f * pb[cp * 3 + 0]);
                 bc[m][1] = fadd(0.5f * pb[c * 3 + 1], 0.5f * __ldg(bjp + c * 3 + 1));
                 bc[m][2] = fadd(0.5f * pb[c * 3 + 2], 0.5f * __ldg(bkp + c * 3 + 2));
             } else {
@@ -161,9 +167,10 @@ fluidx_kernel(FluidxArgs a)
         const float *sb0 = SB + (size_t)q * bs, *sb1 = SB + (size_t)(q + 1) * bs;
 #pragma unroll
         for (int m = 0; m < CPL; ++m) {
-            const int c = tm.cell[m];
-            if (live && tm.valid[m]) {
-                bc[m][0] = fadd(0.5f * sb0[c * 3 + 0], 0.5f * sb0[tm.ip[m] * 3 + 0]);
+            const int c = tm.ci(m);
+            const int cp = (c + 1 == n) ? 0 : c + 1;
+            if (live && tm.valid(m)) {
+                bc[m][0] = fadd(0.5f * sb0[c * 3 + 0], 0.5f * sb0[cp * 3 + 0]);
                 bc[m][1] = fadd(0.5f * sb0[c * 3 + 1], 0.5f * sb1[c * 3 + 1]);
                 bc[m][2] = fadd(0.5f * sb0[c * 3 + 2], 0.5f * SK[c * ks + q]);
             } else {
@@ -178,44 +185,45 @@ fluidx_kernel(FluidxArgs a)
     float u1[CPL][5];
 
     // ================= half step =================
+    // rows 0-4: wl = u - v/c ; rows 5-9: flux
     {
         float v[CPL][5];
         float cl = 0.0f;
 #pragma unroll
         for (int m = 0; m < CPL; ++m) {
             float uu[5];
-            if (tm.valid[m] && live) {
+            if (tm.valid(m) && live) {
 #pragma unroll
-                for (int ii = 0; ii < 5; ++ii) uu[ii] = us[tm.cell[m] * 5 + ii];
+                for (int ii = 0; ii < 5; ++ii) uu[ii] = us[tm.ci(m) * 5 + ii];
             } else {
                 uu[0] = 1.0f; uu[1] = 0.0f; uu[2] = 0.0f; uu[3] = 0.0f; uu[4] = 1.0f;
             }
             float cs, p;
             cell_flux<M>(uu, bc[m], v[m], cs, p);
-            if (tm.valid[m]) cl = fmaxf(cl, cs);
+            if (tm.valid(m)) cl = fmaxf(cl, cs);
         }
         const float c = tm.pencil_max(cl, rq);
         const bool cpos = c > 0.0f;
         const float yc = cpos ? M::recip(c) : 0.0f;
-        // fr = c(u + v/c) kept in u1[]; wl = u - v/c exchanged in x[0:5n)
+        // fr = c(u + v/c) kept in u1[]; wl exchanged
 #pragma unroll
         for (int m = 0; m < CPL; ++m)
 #pragma unroll
             for (int ii = 0; ii < 5; ++ii) {
-                const float uu = us[tm.cell[m] * 5 + ii];
+                const float uu = us[tm.ci(m) * 5 + ii];
                 const float vv = cpos ? M::divy(v[m][ii], c, yc) : v[m][ii];
                 u1[m][ii] = M::mul(c, M::add(uu, vv));
-                if (tm.valid[m]) x[ii * n + tm.cell[m]] = M::sub(uu, vv);
+                tm.put(X(ii), m, M::sub(uu, vv));
             }
         tm.sync();
-        // flux = (fr - c*cshift(wl,+1))/2, exchanged in x[5n:10n)
+        // flux = (fr - c*cshift(wl,+1))/2
 #pragma unroll
         for (int m = 0; m < CPL; ++m)
 #pragma unroll
             for (int ii = 0; ii < 5; ++ii) {
-                const float fl = M::mul(c, x[ii * n + tm.ip[m]]);
+                const float fl = M::mul(c, X(ii)[tm.ci(m) + 1]);
                 u1[m][ii] = 0.5f * M::sub(u1[m][ii], fl);
-                if (tm.valid[m]) x[(5 + ii) * n + tm.cell[m]] = u1[m][ii];
+                tm.put(X(5 + ii), m, u1[m][ii]);
             }
         tm.sync();
         // u1 = u - (flux - cshift(flux,-1)) dt/2
@@ -223,13 +231,14 @@ fluidx_kernel(FluidxArgs a)
         for (int m = 0; m < CPL; ++m)
 #pragma unroll
             for (int ii = 0; ii < 5; ++ii) {
-                const float d = M::sub(u1[m][ii], x[(5 + ii) * n + tm.im[m]]);
-                u1[m][ii] = M::add(us[tm.cell[m] * 5 + ii], M::mul(-hdt, d));
+                const float d = M::sub(u1[m][ii], X(5 + ii)[tm.ci(m) - 1]);
+                u1[m][ii] = M::add(us[tm.ci(m) * 5 + ii], M::mul(-hdt, d));
             }
     }
-    tm.sync();   // every read of x[5n:10n) is done before it is rewritten
+    tm.sync();   // every read of rows 5-9 is done before they are rewritten
 
     // ================= full step =================
+    // rows 0-4: fr, then the flux ; rows 5-9: wl
     {
         float cl = 0.0f;
         {
@@ -238,7 +247,7 @@ fluidx_kernel(FluidxArgs a)
             for (int m = 0; m < CPL; ++m) {
                 float cs, p;
                 cell_flux<M>(u1[m], bc[m], v[m], cs, p);
-                if (tm.valid[m]) {
+                if (tm.valid(m)) {
                     cl = fmaxf(cl, cs);
                     if (!(p > 0.0f)) bad |= MHD_HEALTH_PRESSURE;
                 }
@@ -247,16 +256,13 @@ fluidx_kernel(FluidxArgs a)
             cl = c;
             const bool cpos = c > 0.0f;
             const float yc = cpos ? M::recip(c) : 0.0f;
-            // exchange fr = c(u1+v) in x[0:5n) and wl = u1-v in x[5n:10n)
 #pragma unroll
             for (int m = 0; m < CPL; ++m)
 #pragma unroll
                 for (int ii = 0; ii < 5; ++ii) {
                     const float vv = cpos ? M::divy(v[m][ii], c, yc) : v[m][ii];
-                    if (tm.valid[m]) {
-                        x[ii * n + tm.cell[m]] = M::mul(c, M::add(u1[m][ii], vv));
-                        x[(5 + ii) * n + tm.cell[m]] = M::sub(u1[m][ii], vv);
-                    }
+                    tm.put(X(ii), m, M::mul(c, M::add(u1[m][ii], vv)));
+                    tm.put(X(5 + ii), m, M::sub(u1[m][ii], vv));
                 }
         }
         const float c = cl;
@@ -270,33 +276,31 @@ fluidx_kernel(FluidxArgs a)
         for (int m = 0; m < CPL; ++m)
 #pragma unroll
             for (int ii = 0; ii < 5; ++ii) {
-                const float f0 = x[ii * n + tm.cell[m]];
-                const float frp = x[ii * n + tm.ip[m]];
-                const float frm = x[ii * n + tm.im[m]];
-                const float dfr = M::slope(M::sub(frp, f0), M::sub(f0, frm));
-                const float fl0 = M::mul(c, x[(5 + ii) * n + tm.ip[m]]);
-                const float flp = M::mul(c, x[(5 + ii) * n + tm.ipp[m]]);
-                const float flm = M::mul(c, x[(5 + ii) * n + tm.cell[m]]);
+                const float *fr = X(ii) + tm.ci(m), *wl = X(5 + ii) + tm.ci(m);
+                const float f0 = fr[0];
+                const float dfr = M::slope(M::sub(fr[1], f0), M::sub(f0, fr[-1]));
+                const float fl0 = M::mul(c, wl[1]);
+                const float flp = M::mul(c, wl[2]);
+                const float flm = M::mul(c, wl[0]);
                 const float dfl = M::slope(M::sub(fl0, flp), M::sub(flm, fl0));
                 fx[m][ii] = 0.5f * M::add(M::sub(f0, fl0), M::sub(dfr, dfl));
             }
         tm.sync();
 #pragma unroll
         for (int m = 0; m < CPL; ++m)
-            if (tm.valid[m])
 #pragma unroll
-                for (int ii = 0; ii < 5; ++ii) x[ii * n + tm.cell[m]] = fx[m][ii];
+            for (int ii = 0; ii < 5; ++ii) tm.put(X(ii), m, fx[m][ii]);
         tm.sync();
         // u = u - (flux - cshift(flux,-1)) dt, written back into US
         const float mdt = -dt;
 #pragma unroll
         for (int m = 0; m < CPL; ++m) {
-            if (!(live && tm.valid[m])) continue;
-            const int cc = tm.cell[m];
+            if (!(live && tm.valid(m))) continue;
+            const int cc = tm.ci(m);
             float s = 0.0f, r = 0.0f;
 #pragma unroll
             for (int ii = 0; ii < 5; ++ii) {
-                const float d = M::sub(fx[m][ii], x[ii * n + tm.im[m]]);
+                const float d = M::sub(fx[m][ii], X(ii)[cc - 1]);
                 const float un = M::add(us[cc * 5 + ii], M::mul(mdt, d));
                 us[cc * 5 + ii] = un;
                 s += un;
@@ -335,7 +339,7 @@ fluidx_kernel(FluidxArgs a)
 
 // Launch one instantiation; sets the dynamic shared-memory attribute once per
 // instantiation when above the 48 KB default.
-template <int CPL, int WPP, class M, bool ROWS>
+template <int CPL, int WPP, class M, bool ROWS, int NT>
 cudaError_t launch_fluidx_inst(const FluidxArgs &a, int ppc, cudaStream_t s)
 {
     static size_t smem_set = 0;
@@ -345,25 +349,35 @@ cudaError_t launch_fluidx_inst(const FluidxArgs &a, int ppc, cudaStream_t s)
     const size_t smem = sizeof(float) * (size_t)fx_smem_floats(a.f.n, ppc, WPP, ROWS);
     if (smem > 227 * 1024) return cudaErrorInvalidConfiguration;
     if (smem > 48 * 1024 && smem_set < smem) {
-        cudaError_t e = cudaFuncSetAttribute(fluidx_kernel<CPL, WPP, M, ROWS>,
+        cudaError_t e = cudaFuncSetAttribute(fluidx_kernel<CPL, WPP, M, ROWS, NT>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         smem_set = smem;
     }
-    fluidx_kernel<CPL, WPP, M, ROWS><<<(unsigned)blocks, threads, smem, s>>>(a);
+    fluidx_kernel<CPL, WPP, M, ROWS, NT><<<(unsigned)blocks, threads, smem, s>>>(a);
     return cudaGetLastError();
 }
 
-// dispatch over the supported team shapes and both staging modes (rows mode
-// when the frame's pencils run across memory, sj == 1 and si != 1)
+// dispatch over the supported team shapes, both staging modes (rows mode
+// when the frame's pencils run across memory, sj == 1 and si != 1) and the
+// compile-time length when the pencil fills the team exactly
+template <int C, int W, class M>
+cudaError_t launch_fluidx_shape(const FluidxArgs &a, int ppc, bool rows, cudaStream_t s)
+{
+    constexpr int CAP = 32 * W * C;
+    if (a.f.n == CAP)
+        return rows ? launch_fluidx_inst<C, W, M, true, CAP>(a, ppc, s)
+                    : launch_fluidx_inst<C, W, M, false, CAP>(a, ppc, s);
+    return rows ? launch_fluidx_inst<C, W, M, true, 0>(a, ppc, s)
+                : launch_fluidx_inst<C, W, M, false, 0>(a, ppc, s);
+}
+
 template <class M>
 cudaError_t launch_fluidx_policy(const FluidxArgs &a, const PencilCfg &cfg, cudaStream_t s)
 {
     const bool rows = a.f.si != 1;
-#define MHD_FX(C, W)                                                                  \
-    if (cfg.cpl == C && cfg.wpp == W)                                                 \
-        return rows ? launch_fluidx_inst<C, W, M, true>(a, cfg.ppc, s)                \
-                    : launch_fluidx_inst<C, W, M, false>(a, cfg.ppc, s);
+#define MHD_FX(C, W) \
+    if (cfg.cpl == C && cfg.wpp == W) return launch_fluidx_shape<C, W, M>(a, cfg.ppc, rows, s);
     MHD_PENCIL_SHAPES(MHD_FX)
 #undef MHD_FX
     return cudaErrorInvalidConfiguration;

@@ -8,7 +8,7 @@
 #include <stdint.h>
 
 #include "mhd_math.cuh"
-#include "../../include/mhdgpu.h"
+#include "mhdgpu.h"   // include/ is on the include path (build.py)
 
 namespace mhd {
 
@@ -63,31 +63,48 @@ __host__ __device__ __forceinline__ int nib(unsigned m, int f) { return (int)((m
 
 // A team of TPP = 32*WPP threads owns one pencil; thread t holds the CPL
 // cells c = m*TPP + t (m < CPL).  Cells >= n are padding: they compute on
-// harmless values and are never reduced or stored.
-template <int CPL, int WPP>
+// harmless values and are never reduced or stored.  NT > 0 is the pencil
+// length known at compile time; when it equals the team's capacity (FULL)
+// every slot is a cell and all index arithmetic folds into constants.
+//
+// Stencil exchange rows: one component of the pencil at cells -1 .. n+1,
+// stored from row[-1], so the periodic neighbours c-1, c+1, c+2 of any cell
+// are fixed offsets from c.  put() writes a cell and, for cells n-1, 0 and 1,
+// their periodic copies at -1, n and n+1.  A row takes rs() = n+3 floats.
+template <int CPL, int WPP, int NT = 0>
 struct Team {
     static constexpr int TPP = 32 * WPP;
+    static constexpr bool FULL = NT > 0 && NT == TPP * CPL;
     int t;      // thread within the team
     int n;      // pencil length
-    int cell[CPL];
-    int ip[CPL], im[CPL], ipp[CPL];
-    bool valid[CPL];
 
     __device__ void init(int t_, int n_)
     {
         t = t_;
-        n = n_;
-#pragma unroll
-        for (int m = 0; m < CPL; ++m) {
-            int c = m * TPP + t;
-            valid[m] = c < n;
-            if (!valid[m]) c = 0;
-            cell[m] = c;
-            int a = c + 1; if (a >= n) a -= n;
-            int b = a + 1; if (b >= n) b -= n;
-            ip[m] = a;
-            ipp[m] = b;
-            im[m] = (c == 0) ? n - 1 : c - 1;
+        n = NT > 0 ? NT : n_;
+    }
+    __device__ __forceinline__ int len() const { return NT > 0 ? NT : n; }
+    __device__ __forceinline__ int rs() const { return len() + 3; }
+    __device__ __forceinline__ bool valid(int m) const { return FULL || m * TPP + t < len(); }
+    // the slot's cell, or cell 0 for a padding slot (a safe address)
+    __device__ __forceinline__ int ci(int m) const
+    {
+        return FULL ? m * TPP + t : (m * TPP + t < len() ? m * TPP + t : 0);
+    }
+    __device__ __forceinline__ void put(float *row, int m, float v) const
+    {
+        if (!valid(m)) return;
+        const int c = m * TPP + t;
+        const int nn = len();
+        row[c] = v;
+        if (FULL) {
+            if (m == CPL - 1 && t == TPP - 1) row[-1] = v;
+            if (m == 0 && t == 0) row[nn] = v;
+            if (m == 0 && t == 1) row[nn + 1] = v;
+        } else {
+            if (c == nn - 1) row[-1] = v;
+            if (c == 0) row[nn] = v;
+            if (c == (nn > 1 ? 1 : 0)) row[nn + 1] = v;
         }
     }
 

@@ -11,7 +11,7 @@
 
 #include <vector>
 
-#include "../../include/mhdgpu.h"
+#include "mhdgpu.h"
 #include "profiler.cuh"
 
 struct mhdgpu_profiler {
