@@ -55,6 +55,8 @@ typedef struct CUstream_st *mhdgpu_stream_t;
                                     reference solver runs through it (it takes |.| in
                                     the fast speed, C/mhdflux.c:45), and so does this
                                     one.  Only NONFINITE and DENSITY fail a run. */
+#define MHD_HEALTH_STALL     8u  /* batched kernel: a dependency wait gave up (about
+                                    two seconds); the batch's state is invalid */
 
 /* largest pencil the device kernels accept (cells along the frame's x) */
 #define MHD_MAX_PENCIL      1024
@@ -224,6 +226,52 @@ int mhdgpu_get_tile(int kclass, int n, int *cpl, int *wpp, int *ppc);
 int mhdgpu_autotune(int nx, int ny, int nz, int math);
 
 /* ------------------------------------------------------------------------
+ * Batched ensemble (no counterpart in the reference, whose drivers advance
+ * one box: Heterogeneous_MHD/C/mhd.c:59-125).  Many independent periodic
+ * boxes, each with its own sizes (1 .. MHD_BATCH_MAX_PENCIL cells on every
+ * axis; non-cubic and uneven allowed), state, clock and dt, advance together.
+ * A step is one CFL launch over all boxes, one clock launch and one persistent
+ * launch per sweep (x, y, z, z, y, x), whatever the number of boxes; each box
+ * goes through the transpose-free step of mhdgpu_step_fused and ends bit for
+ * bit where mhdgpu_advance(path = MHD_PATH_FUSED) takes it alone.
+ *
+ * The state of box i stays in the caller's device arrays d_u[i] (5 floats
+ * per cell) and d_b[i] (3 per cell), reference layout; the handle keeps the
+ * pointers.  mhdgpu_batch_create allocates the handle's device memory
+ * (mhdgpu_batch_workspace_bytes: 8 bytes per cell plus small tables) and
+ * synchronises; nothing else allocates.  tf (host, nbox floats, or NULL for
+ * none) is each box's end time, with the dt clamp and dt = 0 after the end as
+ * in mhdgpu_advance.  Clocks start at t = 0.
+ * ------------------------------------------------------------------------ */
+#define MHD_BATCH_MAX_PENCIL 256
+#define MHD_BATCH_MAX_BOXES  65536
+
+typedef struct mhdgpu_batch mhdgpu_batch;
+size_t mhdgpu_batch_workspace_bytes(int nbox, const int *dims /* 3*nbox: nx,ny,nz */);
+int mhdgpu_batch_create(mhdgpu_batch **out, int nbox, const int *dims, float *const *d_u,
+                        float *const *d_b, double cfl_number, int cfl_mode, const float *tf);
+int mhdgpu_batch_destroy(mhdgpu_batch *bt);
+/* enqueues nsteps steps on stream (8 launches per step; capturable into a
+ * CUDA graph, no host synchronisation) */
+int mhdgpu_batch_advance(mhdgpu_batch *bt, int nsteps, mhdgpu_stream_t stream);
+/* synchronises stream and copies the nbox clocks to the host; returns
+ * MHD_ERR_TIMEOUT after a stall, MHD_ERR_UNPHYSICAL when a box's health
+ * reports NaN/Inf or rho <= 0 */
+int mhdgpu_batch_read_clocks(mhdgpu_batch *bt, mhdgpu_clock *clocks, mhdgpu_stream_t stream);
+/* Block schedule of the sweeps along one axis (0, 1, 2): threads per CTA
+ * (64, 128 or 256; a CTA holds threads/32 pencils of length <= 128 or half as
+ * many longer ones) and resident CTAs per SM (the persistent grid is
+ * SMs x ctas_per_sm, capped by the occupancy the kernel allows).  Synchronous
+ * (uploads the work tables); not under stream capture. */
+int mhdgpu_batch_set_schedule(mhdgpu_batch *bt, int axis, int threads, int ctas_per_sm);
+int mhdgpu_batch_get_schedule(const mhdgpu_batch *bt, int axis, int *threads, int *ctas_per_sm);
+/* Autotuner: times every schedule on this batch's own boxes (one warm-up and
+ * two timed steps each, CUDA events per sweep), keeps the fastest per axis and
+ * restores the boxes' state and clocks.  Allocates a snapshot of the state
+ * for the duration; synchronises.  Not under stream capture. */
+int mhdgpu_batch_tune(mhdgpu_batch *bt, mhdgpu_stream_t stream);
+
+/* ------------------------------------------------------------------------
  * Profiler: per-kernel-class device time from CUDA events.  While a profiler
  * is attached to the calling thread, every entry above records a start and
  * an end event on its stream around its launches (no added synchronisation;
@@ -234,7 +282,8 @@ int mhdgpu_autotune(int nx, int ny, int nz, int math);
 #define MHD_KCLASS_ADVECT     1   /* advectbyzx flux kernel + b_x gather kernel */
 #define MHD_KCLASS_TRANSPOSE  2   /* transpose12 / transpose13 */
 #define MHD_KCLASS_CFL        3   /* CFL reduction (+ its clock/finish kernel) */
-#define MHD_KCLASS_COUNT      4
+#define MHD_KCLASS_BATCH      4   /* batched ensemble sweeps (mhdgpu_batch_advance) */
+#define MHD_KCLASS_COUNT      5
 
 typedef struct mhdgpu_profiler mhdgpu_profiler;
 int mhdgpu_profiler_create(mhdgpu_profiler **p, int max_records);

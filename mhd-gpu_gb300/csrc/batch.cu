@@ -1,0 +1,482 @@
+// batch.cu - host side of the batched ensemble (include/mhdgpu.h,
+// mhdgpu_batch_*): work tables, the per-step launch sequence, the block
+// schedule and its autotuner, plus the CFL and clock kernels over all boxes.
+// The sweep kernels are in batch_kernel.cuh (instantiated per math policy in
+// batch_faithful.cu and batch_fast.cu).
+#include <cuda_runtime.h>
+#include <stdio.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "batch_kernel.cuh"
+#include "profiler.cuh"
+
+namespace mhd {
+
+// CFL over every box: items are (box, chunk of kCflChunk cells) through a
+// prefix table; each CTA reduces its chunk and folds it into the box's word.
+constexpr int kCflThreads = 256;
+constexpr int kCflChunk = kCflThreads * 16;
+
+struct CflWork {
+    const BoxDesc *box;
+    const long long *start;   // nbox + 1 prefix sums of chunk counts
+    int nbox, mode;
+};
+
+__global__ void __launch_bounds__(kCflThreads)
+batch_cfl_kernel(CflWork w)
+{
+    const long long total = w.start[w.nbox];
+    for (long long it = blockIdx.x; it < total; it += gridDim.x) {
+        int lo = 0, hi = w.nbox - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (w.start[mid] <= it) lo = mid;
+            else hi = mid - 1;
+        }
+        const BoxDesc d = w.box[lo];
+        const long long ncell = (long long)d.nx * d.ny * d.nz;
+        const long long c0 = (it - w.start[lo]) * kCflChunk;
+        const long long c1 = min(c0 + kCflChunk, ncell);
+        float cl = 0.0f;
+        for (long long c = c0 + threadIdx.x; c < c1; c += blockDim.x)
+            cl = fmaxf(cl, cfl_cell_speed(d.u, d.b, d.nx, d.ny, d.nz, w.mode, c));
+        cfl_block_max(cl, &d.clk->cmax);
+    }
+}
+
+// One clock tick per box, and the sweeps' claim and completion counters
+// cleared for the step.
+__global__ void batch_clock_kernel(const BoxDesc *box, const float *tf, int nbox, double cfl_number,
+                                   unsigned *ctr, int nctr)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    for (int c = i; c < nctr; c += gridDim.x * blockDim.x) ctr[c] = 0u;
+    if (i < nbox) clock_tick(box[i].clk, cfl_number, tf[i], nullptr);
+}
+
+}  // namespace mhd
+
+using namespace mhd;
+
+namespace {
+
+constexpr int kSweepAxis[6] = {0, 1, 2, 2, 1, 0};
+constexpr int kSweepFluidFirst[6] = {1, 1, 1, 0, 0, 0};
+constexpr int kThreadChoices[3] = {64, 128, 256};
+
+}  // namespace
+
+struct mhdgpu_batch {
+    int nbox = 0;
+    int device = 0, num_sms = 0;
+    double cfl_number = 0.0;
+    int cfl_mode = MHD_CFL_C;
+    std::vector<BoxDesc> box;
+    BoxDesc *d_box = nullptr;
+    mhdgpu_clock *d_clk = nullptr;
+    float *d_scr = nullptr;
+    float *d_tf = nullptr;
+    // counters: 6 claims, then 6 x 3*nbox completion counts; then the abort word
+    unsigned *d_ctr = nullptr;
+    int nctr = 0;
+    unsigned *d_abort = nullptr;
+    long long *d_start = nullptr;       // 6 x (3*nbox + 1)
+    long long *d_cfl_start = nullptr;   // nbox + 1
+    long long cfl_total = 0;
+    long long total[6] = {};
+    int threads[3] = {256, 256, 256};
+    int cps[3] = {2, 2, 2};             // requested CTAs per SM
+    int grid[6] = {};
+    size_t smem[3] = {};
+
+    ~mhdgpu_batch()
+    {
+        cudaFree(d_box); cudaFree(d_clk); cudaFree(d_scr); cudaFree(d_tf);
+        cudaFree(d_ctr); cudaFree(d_start); cudaFree(d_cfl_start);
+    }
+};
+
+namespace {
+
+thread_local char g_berr[256];
+
+int bfail(int st, const char *msg)
+{
+    set_last_error(msg);
+    return st;
+}
+
+int bcuda(cudaError_t e, const char *where)
+{
+    snprintf(g_berr, sizeof g_berr, "%s: %s", where, cudaGetErrorString(e));
+    set_last_error(g_berr);
+    return MHD_ERR_CUDA;
+}
+
+#define BCU(call, where)                                      \
+    do {                                                      \
+        cudaError_t e_ = (call);                              \
+        if (e_ != cudaSuccess) return bcuda(e_, where);       \
+    } while (0)
+
+bool dims_ok(int nbox, const int *dims)
+{
+    if (nbox < 1 || nbox > MHD_BATCH_MAX_BOXES || !dims) return false;
+    for (int i = 0; i < 3 * nbox; ++i)
+        if (dims[i] < 1 || dims[i] > kBatchMaxPencil) return false;
+    return true;
+}
+
+long long cells_of(const int *d) { return (long long)d[0] * d[1] * d[2]; }
+
+int occupancy(bool rows, int threads, size_t smem)
+{
+    return math_mode() == MHD_MATH_FAST ? batch_sweep_occupancy_fast(rows, threads, smem)
+                                        : batch_sweep_occupancy_faithful(rows, threads, smem);
+}
+
+// dynamic shared memory of a sweep along axis with `threads` per CTA: the
+// largest tile of any box
+size_t sweep_smem(const mhdgpu_batch &bt, int axis, int threads)
+{
+    long long fl = 0;
+    const bool rows = axis != 0;
+    for (const BoxDesc &d : bt.box) {
+        const Frame f = make_view(axis, d.nx, d.ny, d.nz);
+        const int tpp = batch_tpp(f.n);
+        const int ppc = std::max(1, threads / tpp);
+        fl = std::max(fl, fx_smem_floats(f.n, ppc, tpp / 32, rows));
+        fl = std::max(fl, ax_smem_floats(f.n, ppc, rows));
+    }
+    return sizeof(float) * (size_t)fl;
+}
+
+// (re)builds the work tables of the sweeps and the grid sizes; synchronous
+int build_tables(mhdgpu_batch &bt)
+{
+    const int nb = bt.nbox;
+    std::vector<long long> start(6 * (size_t)(3 * nb + 1));
+    for (int s = 0; s < 6; ++s) {
+        const int axis = kSweepAxis[s];
+        const bool rows = axis != 0;
+        const int threads = bt.threads[axis];
+        long long *st = &start[(size_t)s * (3 * nb + 1)];
+        long long acc = 0;
+        for (int slot = 0; slot < 3; ++slot) {
+            const int ph = batch_phase(slot, kSweepFluidFirst[s]);
+            for (int i = 0; i < nb; ++i) {
+                const BoxDesc &d = bt.box[i];
+                const Frame f = make_view(axis, d.nx, d.ny, d.nz);
+                const int ppc = threads / batch_tpp(f.n);
+                if (ppc < 1)
+                    return bfail(MHD_ERR_ARG, "mhdgpu_batch: fewer threads per CTA than a pencil's team "
+                                              "(64 for pencils of 65-127 cells, 128 above 128)");
+                st[slot * nb + i] = acc;
+                acc += ph == kPhaseB1 ? batch_chunks(f.npen * f.n, threads * 8) : batch_tiles(f, ppc, rows);
+            }
+        }
+        st[3 * nb] = acc;
+        bt.total[s] = acc;
+        if (acc >= (1LL << 31)) return bfail(MHD_ERR_ARG, "mhdgpu_batch: too many work items");
+    }
+    for (int axis = 0; axis < 3; ++axis) {
+        bt.smem[axis] = sweep_smem(bt, axis, bt.threads[axis]);
+        if (bt.smem[axis] > 227 * 1024) return bfail(MHD_ERR_ARG, "mhdgpu_batch: tile exceeds shared memory");
+        const int occ = occupancy(axis != 0, bt.threads[axis], bt.smem[axis]);
+        if (occ < 1) return bfail(MHD_ERR_CUDA, "mhdgpu_batch: the sweep kernel cannot be resident");
+        const int cps = std::min(bt.cps[axis], occ);
+        for (int s = 0; s < 6; ++s)
+            if (kSweepAxis[s] == axis)
+                bt.grid[s] = (int)std::max(1LL, std::min((long long)bt.num_sms * cps, bt.total[s]));
+    }
+    BCU(cudaMemcpy(bt.d_start, start.data(), start.size() * sizeof(long long), cudaMemcpyHostToDevice),
+        "mhdgpu_batch tables");
+    return MHD_OK;
+}
+
+int launch_step(mhdgpu_batch &bt, cudaStream_t s, cudaEvent_t *ev /* 7 events or NULL */)
+{
+    const int nb = bt.nbox;
+    {
+        ProfScope ps(MHD_KCLASS_CFL, 2, s);
+        CflWork cw{bt.d_box, bt.d_cfl_start, nb, bt.cfl_mode};
+        const int g = (int)std::max(1LL, std::min((long long)bt.num_sms * 8, bt.cfl_total));
+        batch_cfl_kernel<<<g, kCflThreads, 0, s>>>(cw);
+        BCU(cudaGetLastError(), "mhdgpu_batch_advance cfl");
+        const int gc = (std::max(nb, bt.nctr) + 255) / 256;
+        batch_clock_kernel<<<gc, 256, 0, s>>>(bt.d_box, bt.d_tf, nb, bt.cfl_number, bt.d_ctr, bt.nctr);
+        BCU(cudaGetLastError(), "mhdgpu_batch_advance clock");
+    }
+    const int math = math_mode();
+    for (int sw = 0; sw < 6; ++sw) {
+        const int axis = kSweepAxis[sw];
+        SweepWork w;
+        w.box = bt.d_box;
+        w.start = bt.d_start + (size_t)sw * (3 * nb + 1);
+        w.claim = bt.d_ctr + sw;
+        w.done = bt.d_ctr + 6 + (size_t)sw * 3 * nb;
+        w.abort = bt.d_abort;
+        w.nbox = nb;
+        w.axis = axis;
+        w.fluid_first = kSweepFluidFirst[sw];
+        w.b1_chunk = bt.threads[axis] * 8;
+        if (ev) BCU(cudaEventRecord(ev[sw], s), "mhdgpu_batch event");
+        ProfScope ps(MHD_KCLASS_BATCH, 1, s);
+        const cudaError_t e =
+            math == MHD_MATH_FAST
+                ? launch_batch_sweep_fast(w, axis != 0, bt.grid[sw], bt.threads[axis], bt.smem[axis], s)
+                : launch_batch_sweep_faithful(w, axis != 0, bt.grid[sw], bt.threads[axis], bt.smem[axis], s);
+        BCU(e, "mhdgpu_batch_advance sweep");
+    }
+    if (ev) BCU(cudaEventRecord(ev[6], s), "mhdgpu_batch event");
+    return MHD_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+size_t mhdgpu_batch_workspace_bytes(int nbox, const int *dims)
+{
+    if (!dims_ok(nbox, dims)) return 0;
+    long long cells = 0;
+    for (int i = 0; i < nbox; ++i) cells += cells_of(dims + 3 * i);
+    const size_t nctr = 6 + 18 * (size_t)nbox + 1;
+    return sizeof(float) * 2 * (size_t)cells + nbox * (sizeof(BoxDesc) + sizeof(mhdgpu_clock) + sizeof(float)) +
+           nctr * sizeof(unsigned) + (6 * (3 * (size_t)nbox + 1) + nbox + 1) * sizeof(long long);
+}
+
+int mhdgpu_batch_create(mhdgpu_batch **out, int nbox, const int *dims, float *const *d_u,
+                        float *const *d_b, double cfl_number, int cfl_mode, const float *tf)
+{
+    if (!out) return bfail(MHD_ERR_ARG, "mhdgpu_batch_create: null handle pointer");
+    *out = nullptr;
+    if (!dims_ok(nbox, dims))
+        return bfail(MHD_ERR_ARG, "mhdgpu_batch_create: need 1..65536 boxes, each axis 1..MHD_BATCH_MAX_PENCIL");
+    if (!d_u || !d_b) return bfail(MHD_ERR_ARG, "mhdgpu_batch_create: null state table");
+    for (int i = 0; i < nbox; ++i)
+        if (!d_u[i] || !d_b[i]) return bfail(MHD_ERR_ARG, "mhdgpu_batch_create: null box state");
+    if (!(cfl_number > 0.0)) return bfail(MHD_ERR_ARG, "mhdgpu_batch_create: cfl_number must be > 0");
+    if (cfl_mode != MHD_CFL_C && cfl_mode != MHD_CFL_AVERAGED)
+        return bfail(MHD_ERR_ARG, "mhdgpu_batch_create: bad cfl mode");
+    mhdgpu_batch *bt = new mhdgpu_batch;
+    bt->nbox = nbox;
+    bt->cfl_number = cfl_number;
+    bt->cfl_mode = cfl_mode;
+    cudaError_t e = cudaGetDevice(&bt->device);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&bt->num_sms, cudaDevAttrMultiProcessorCount, bt->device);
+    long long cells = 0;
+    std::vector<long long> cfl_start(nbox + 1);
+    for (int i = 0; i < nbox; ++i) {
+        cfl_start[i] = bt->cfl_total;
+        const long long nc = cells_of(dims + 3 * i);
+        bt->cfl_total += batch_chunks(nc, kCflChunk);
+        cells += nc;
+    }
+    cfl_start[nbox] = bt->cfl_total;
+    bt->nctr = 6 + 18 * nbox;
+    std::vector<float> htf(nbox, 0.0f);
+    if (tf) std::copy(tf, tf + nbox, htf.begin());
+    if (e == cudaSuccess) e = cudaMalloc(&bt->d_box, nbox * sizeof(BoxDesc));
+    if (e == cudaSuccess) e = cudaMalloc(&bt->d_clk, nbox * sizeof(mhdgpu_clock));
+    if (e == cudaSuccess) e = cudaMalloc(&bt->d_scr, 2 * sizeof(float) * (size_t)cells);
+    if (e == cudaSuccess) e = cudaMalloc(&bt->d_tf, nbox * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc(&bt->d_ctr, (bt->nctr + 1) * sizeof(unsigned));
+    if (e == cudaSuccess) e = cudaMalloc(&bt->d_start, 6 * (3 * (size_t)nbox + 1) * sizeof(long long));
+    if (e == cudaSuccess) e = cudaMalloc(&bt->d_cfl_start, (nbox + 1) * sizeof(long long));
+    if (e != cudaSuccess) {
+        delete bt;
+        return bcuda(e, "mhdgpu_batch_create");
+    }
+    bt->d_abort = bt->d_ctr + bt->nctr;
+    bt->box.resize(nbox);
+    long long off = 0;
+    for (int i = 0; i < nbox; ++i) {
+        BoxDesc &d = bt->box[i];
+        d.u = d_u[i];
+        d.b = d_b[i];
+        d.scr = bt->d_scr + 2 * off;
+        d.clk = bt->d_clk + i;
+        d.nx = dims[3 * i];
+        d.ny = dims[3 * i + 1];
+        d.nz = dims[3 * i + 2];
+        d.pad = 0;
+        off += cells_of(dims + 3 * i);
+    }
+    e = cudaMemcpy(bt->d_box, bt->box.data(), nbox * sizeof(BoxDesc), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemset(bt->d_clk, 0, nbox * sizeof(mhdgpu_clock));
+    if (e == cudaSuccess) e = cudaMemset(bt->d_ctr, 0, (bt->nctr + 1) * sizeof(unsigned));
+    if (e == cudaSuccess) e = cudaMemcpy(bt->d_tf, htf.data(), nbox * sizeof(float), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(bt->d_cfl_start, cfl_start.data(), (nbox + 1) * sizeof(long long), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        delete bt;
+        return bcuda(e, "mhdgpu_batch_create");
+    }
+    const int st = build_tables(*bt);
+    if (st != MHD_OK) {
+        delete bt;
+        return st;
+    }
+    *out = bt;
+    return MHD_OK;
+}
+
+int mhdgpu_batch_destroy(mhdgpu_batch *bt)
+{
+    if (!bt) return bfail(MHD_ERR_ARG, "mhdgpu_batch_destroy: null handle");
+    delete bt;
+    return MHD_OK;
+}
+
+int mhdgpu_batch_advance(mhdgpu_batch *bt, int nsteps, mhdgpu_stream_t stream)
+{
+    if (!bt) return bfail(MHD_ERR_ARG, "mhdgpu_batch_advance: null handle");
+    if (nsteps < 0) return bfail(MHD_ERR_ARG, "mhdgpu_batch_advance: nsteps < 0");
+    for (int it = 0; it < nsteps; ++it) {
+        const int st = launch_step(*bt, (cudaStream_t)stream, nullptr);
+        if (st) return st;
+    }
+    return MHD_OK;
+}
+
+int mhdgpu_batch_read_clocks(mhdgpu_batch *bt, mhdgpu_clock *clocks, mhdgpu_stream_t stream)
+{
+    if (!bt || !clocks) return bfail(MHD_ERR_ARG, "mhdgpu_batch_read_clocks: null pointer");
+    cudaStream_t s = (cudaStream_t)stream;
+    unsigned abort_word = 0;
+    BCU(cudaMemcpyAsync(clocks, bt->d_clk, bt->nbox * sizeof(mhdgpu_clock), cudaMemcpyDeviceToHost, s),
+        "mhdgpu_batch_read_clocks");
+    BCU(cudaMemcpyAsync(&abort_word, bt->d_abort, sizeof(unsigned), cudaMemcpyDeviceToHost, s),
+        "mhdgpu_batch_read_clocks");
+    BCU(cudaStreamSynchronize(s), "mhdgpu_batch_read_clocks");
+    if (abort_word) return bfail(MHD_ERR_TIMEOUT, "mhdgpu_batch: a dependency wait gave up; the state is invalid");
+    for (int i = 0; i < bt->nbox; ++i)
+        if (clocks[i].health & (MHD_HEALTH_NONFINITE | MHD_HEALTH_DENSITY))
+            return bfail(MHD_ERR_UNPHYSICAL, "mhdgpu_batch: a box reports NaN/Inf or rho <= 0");
+    return MHD_OK;
+}
+
+int mhdgpu_batch_set_schedule(mhdgpu_batch *bt, int axis, int threads, int ctas_per_sm)
+{
+    if (!bt) return bfail(MHD_ERR_ARG, "mhdgpu_batch_set_schedule: null handle");
+    if (axis < 0 || axis > 2) return bfail(MHD_ERR_ARG, "mhdgpu_batch_set_schedule: axis must be 0, 1 or 2");
+    if (threads != 64 && threads != 128 && threads != 256)
+        return bfail(MHD_ERR_ARG, "mhdgpu_batch_set_schedule: threads must be 64, 128 or 256");
+    if (ctas_per_sm < 1 || ctas_per_sm > 32)
+        return bfail(MHD_ERR_ARG, "mhdgpu_batch_set_schedule: ctas_per_sm must be 1..32");
+    const int old_t = bt->threads[axis], old_c = bt->cps[axis];
+    bt->threads[axis] = threads;
+    bt->cps[axis] = ctas_per_sm;
+    const int st = build_tables(*bt);
+    if (st != MHD_OK) {
+        bt->threads[axis] = old_t;
+        bt->cps[axis] = old_c;
+        build_tables(*bt);
+    }
+    return st;
+}
+
+int mhdgpu_batch_get_schedule(const mhdgpu_batch *bt, int axis, int *threads, int *ctas_per_sm)
+{
+    if (!bt || axis < 0 || axis > 2) return bfail(MHD_ERR_ARG, "mhdgpu_batch_get_schedule: bad argument");
+    if (threads) *threads = bt->threads[axis];
+    if (ctas_per_sm) *ctas_per_sm = bt->cps[axis];
+    return MHD_OK;
+}
+
+int mhdgpu_batch_tune(mhdgpu_batch *bt, mhdgpu_stream_t stream)
+{
+    if (!bt) return bfail(MHD_ERR_ARG, "mhdgpu_batch_tune: null handle");
+    cudaStream_t s = (cudaStream_t)stream;
+    const int nb = bt->nbox;
+    // snapshot of the state and the clocks
+    long long cells = 0;
+    for (const BoxDesc &d : bt->box) cells += (long long)d.nx * d.ny * d.nz;
+    float *snap = nullptr;
+    mhdgpu_clock *csnap = nullptr;
+    BCU(cudaMalloc(&snap, 8 * sizeof(float) * (size_t)cells), "mhdgpu_batch_tune");
+    if (cudaMalloc(&csnap, nb * sizeof(mhdgpu_clock)) != cudaSuccess) {
+        cudaFree(snap);
+        return bcuda(cudaErrorMemoryAllocation, "mhdgpu_batch_tune");
+    }
+    cudaEvent_t ev[7] = {};
+    int st = MHD_OK;
+    cudaError_t e = cudaSuccess;
+    for (int i = 0; i < 7 && e == cudaSuccess; ++i) e = cudaEventCreate(&ev[i]);
+    long long off = 0;
+    for (int i = 0; i < nb && e == cudaSuccess; ++i) {
+        const BoxDesc &d = bt->box[i];
+        const size_t nc = (size_t)d.nx * d.ny * d.nz;
+        e = cudaMemcpyAsync(snap + 8 * off, d.u, 5 * nc * sizeof(float), cudaMemcpyDeviceToDevice, s);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(snap + 8 * off + 5 * nc, d.b, 3 * nc * sizeof(float), cudaMemcpyDeviceToDevice, s);
+        off += nc;
+    }
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(csnap, bt->d_clk, nb * sizeof(mhdgpu_clock), cudaMemcpyDeviceToDevice, s);
+    if (e != cudaSuccess) st = bcuda(e, "mhdgpu_batch_tune");
+    const int keep_t[3] = {bt->threads[0], bt->threads[1], bt->threads[2]};
+    const int keep_c[3] = {bt->cps[0], bt->cps[1], bt->cps[2]};
+    float best[3] = {1e30f, 1e30f, 1e30f};
+    int best_t[3] = {keep_t[0], keep_t[1], keep_t[2]}, best_c[3] = {keep_c[0], keep_c[1], keep_c[2]};
+    for (int ti = 0; ti < 3 && st == MHD_OK; ++ti) {
+        for (int cps = 1; cps <= 4 && st == MHD_OK; ++cps) {
+            for (int a = 0; a < 3; ++a) {
+                bt->threads[a] = kThreadChoices[ti];
+                bt->cps[a] = cps;
+            }
+            if (build_tables(*bt) != MHD_OK) continue;   // this schedule does not fit: skip it
+            float tsum[3] = {0, 0, 0};
+            for (int rep = 0; rep < 3 && st == MHD_OK; ++rep) {
+                st = launch_step(*bt, s, ev);
+                if (st != MHD_OK) break;
+                if ((e = cudaEventSynchronize(ev[6])) != cudaSuccess) { st = bcuda(e, "mhdgpu_batch_tune"); break; }
+                if (rep == 0) continue;   // warm-up
+                for (int sw = 0; sw < 6; ++sw) {
+                    float ms = 0.0f;
+                    cudaEventElapsedTime(&ms, ev[sw], ev[sw + 1]);
+                    tsum[kSweepAxis[sw]] += ms;
+                }
+            }
+            for (int a = 0; a < 3; ++a) {
+                if (tsum[a] < best[a]) {
+                    best[a] = tsum[a];
+                    best_t[a] = kThreadChoices[ti];
+                    best_c[a] = cps;
+                }
+            }
+        }
+    }
+    for (int a = 0; a < 3; ++a) {
+        bt->threads[a] = st == MHD_OK ? best_t[a] : keep_t[a];
+        bt->cps[a] = st == MHD_OK ? best_c[a] : keep_c[a];
+    }
+    const int st2 = build_tables(*bt);
+    // restore the state, the clocks and the counters
+    off = 0;
+    e = cudaSuccess;
+    for (int i = 0; i < nb && e == cudaSuccess; ++i) {
+        const BoxDesc &d = bt->box[i];
+        const size_t nc = (size_t)d.nx * d.ny * d.nz;
+        e = cudaMemcpyAsync(d.u, snap + 8 * off, 5 * nc * sizeof(float), cudaMemcpyDeviceToDevice, s);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(d.b, snap + 8 * off + 5 * nc, 3 * nc * sizeof(float), cudaMemcpyDeviceToDevice, s);
+        off += nc;
+    }
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(bt->d_clk, csnap, nb * sizeof(mhdgpu_clock), cudaMemcpyDeviceToDevice, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    for (int i = 0; i < 7; ++i)
+        if (ev[i]) cudaEventDestroy(ev[i]);
+    cudaFree(snap);
+    cudaFree(csnap);
+    if (st != MHD_OK) return st;
+    if (e != cudaSuccess) return bcuda(e, "mhdgpu_batch_tune restore");
+    return st2;
+}
+
+}  // extern "C"

@@ -52,9 +52,11 @@ __host__ __device__ inline long long fx_smem_floats(int n, int ppc, int wpp, boo
     return (long long)ppc * fx_ps(n, rows) + fx_xsize(n, ppc, rows) + (long long)ppc * wpp;
 }
 
+// One CTA's work: tile = the CTA's group of pencils (contiguous mode: pencils
+// tile*ppc ..; rows mode: j-block tile % njb of plane tile / njb).  Called once
+// per CTA by fluidx_kernel and in a loop by the batched kernel (batch.cu).
 template <int CPL, int WPP, class M, bool ROWS, int NT>
-__global__ void __launch_bounds__(256)
-fluidx_kernel(FluidxArgs a)
+__device__ __forceinline__ void fluidx_tile(const FluidxArgs &a, long long tile)
 {
     constexpr int TPP = 32 * WPP;
     extern __shared__ float smem[];
@@ -70,12 +72,12 @@ fluidx_kernel(FluidxArgs a)
     int j0 = 0, k = 0;         // ROWS: first j and the plane
     int nvalid;
     if (!ROWS) {
-        p0 = (long long)blockIdx.x * ppc;
+        p0 = tile * ppc;
         nvalid = (int)min((long long)ppc, f.npen - p0);
     } else {
         const int njb = (f.ny + ppc - 1) / ppc;
-        k = blockIdx.x / njb;
-        j0 = (blockIdx.x - k * njb) * ppc;
+        k = (int)(tile / njb);
+        j0 = (int)(tile - (long long)k * njb) * ppc;
         nvalid = min(ppc, f.ny - j0);
     }
     const bool live = q < nvalid;
@@ -103,7 +105,9 @@ fluidx_kernel(FluidxArgs a)
         block_copy_in(XA, a.b + p0 * 3 * n, (long long)nvalid * 3 * n, threadIdx.x, blockDim.x);
         __syncthreads();
         // b3x = b/2 ; b3x(1) += cshift(b3x(1),1) ; b3x(2) += b(2,jp)/2 ;
-        // b3x(3) += b(3,kp)/2   (fluidx.c:71-81; the halvings are exact)
+        // b3x(3) += b(3,kp)/2   (fluidx.c:71-81; the halvings are exact).
+        // Plain coherent loads, not the read-only path: the batched sweep
+        // kernel writes b earlier in the same launch.
         const int jp = (jq + 1 == f.ny) ? 0 : jq + 1;
         const int kp = (kq + 1 == f.nz) ? 0 : kq + 1;
         const float *bjp = a.b + ((long long)kq * f.ny + jp) * 3 * n;
@@ -115,8 +119,8 @@ fluidx_kernel(FluidxArgs a)
             const int cp = (c + 1 == n) ? 0 : c + 1;
             if (live && tm.valid(m)) {
                 bc[m][0] = fadd(0.5f * pb[c * 3 + 0], 0.5f * pb[cp * 3 + 0]);
-                bc[m][1] = fadd(0.5f * pb[c * 3 + 1], 0.5f * __ldg(bjp + c * 3 + 1));
-                bc[m][2] = fadd(0.5f * pb[c * 3 + 2], 0.5f * __ldg(bkp + c * 3 + 2));
+                bc[m][1] = fadd(0.5f * pb[c * 3 + 1], 0.5f * bjp[c * 3 + 1]);
+                bc[m][2] = fadd(0.5f * pb[c * 3 + 2], 0.5f * bkp[c * 3 + 2]);
             } else {
                 bc[m][0] = 0.0f; bc[m][1] = 0.0f; bc[m][2] = 0.0f;
             }
@@ -191,8 +195,9 @@ fluidx_kernel(FluidxArgs a)
         float cl = 0.0f;
 #pragma unroll
         for (int m = 0; m < CPL; ++m) {
+            if (!tm.valid(m)) continue;   // padding slots compute nothing
             float uu[5];
-            if (tm.valid(m) && live) {
+            if (live) {
 #pragma unroll
                 for (int ii = 0; ii < 5; ++ii) uu[ii] = us[tm.ci(m) * 5 + ii];
             } else {
@@ -200,7 +205,7 @@ fluidx_kernel(FluidxArgs a)
             }
             float cs, p;
             cell_flux<M>(uu, bc[m], v[m], cs, p);
-            if (tm.valid(m)) cl = fmaxf(cl, cs);
+            cl = fmaxf(cl, cs);
         }
         const float c = tm.pencil_max(cl, rq);
         const bool cpos = c > 0.0f;
@@ -209,7 +214,7 @@ fluidx_kernel(FluidxArgs a)
 #pragma unroll
         for (int m = 0; m < CPL; ++m)
 #pragma unroll
-            for (int ii = 0; ii < 5; ++ii) {
+            for (int ii = 0; ii < 5; ++ii) if (tm.valid(m)) {
                 const float uu = us[tm.ci(m) * 5 + ii];
                 const float vv = cpos ? M::divy(v[m][ii], c, yc) : v[m][ii];
                 u1[m][ii] = M::mul(c, M::add(uu, vv));
@@ -220,7 +225,7 @@ fluidx_kernel(FluidxArgs a)
 #pragma unroll
         for (int m = 0; m < CPL; ++m)
 #pragma unroll
-            for (int ii = 0; ii < 5; ++ii) {
+            for (int ii = 0; ii < 5; ++ii) if (tm.valid(m)) {
                 const float fl = M::mul(c, X(ii)[tm.ci(m) + 1]);
                 u1[m][ii] = 0.5f * M::sub(u1[m][ii], fl);
                 tm.put(X(5 + ii), m, u1[m][ii]);
@@ -230,7 +235,7 @@ fluidx_kernel(FluidxArgs a)
 #pragma unroll
         for (int m = 0; m < CPL; ++m)
 #pragma unroll
-            for (int ii = 0; ii < 5; ++ii) {
+            for (int ii = 0; ii < 5; ++ii) if (tm.valid(m)) {
                 const float d = M::sub(u1[m][ii], X(5 + ii)[tm.ci(m) - 1]);
                 u1[m][ii] = M::add(us[tm.ci(m) * 5 + ii], M::mul(-hdt, d));
             }
@@ -245,12 +250,11 @@ fluidx_kernel(FluidxArgs a)
             float v[CPL][5];
 #pragma unroll
             for (int m = 0; m < CPL; ++m) {
+                if (!tm.valid(m)) continue;
                 float cs, p;
                 cell_flux<M>(u1[m], bc[m], v[m], cs, p);
-                if (tm.valid(m)) {
-                    cl = fmaxf(cl, cs);
-                    if (!(p > 0.0f)) bad |= MHD_HEALTH_PRESSURE;
-                }
+                cl = fmaxf(cl, cs);
+                if (!(p > 0.0f)) bad |= MHD_HEALTH_PRESSURE;
             }
             const float c = tm.pencil_max(cl, rq);
             cl = c;
@@ -259,7 +263,7 @@ fluidx_kernel(FluidxArgs a)
 #pragma unroll
             for (int m = 0; m < CPL; ++m)
 #pragma unroll
-                for (int ii = 0; ii < 5; ++ii) {
+                for (int ii = 0; ii < 5; ++ii) if (tm.valid(m)) {
                     const float vv = cpos ? M::divy(v[m][ii], c, yc) : v[m][ii];
                     tm.put(X(ii), m, M::mul(c, M::add(u1[m][ii], vv)));
                     tm.put(X(5 + ii), m, M::sub(u1[m][ii], vv));
@@ -275,7 +279,7 @@ fluidx_kernel(FluidxArgs a)
 #pragma unroll
         for (int m = 0; m < CPL; ++m)
 #pragma unroll
-            for (int ii = 0; ii < 5; ++ii) {
+            for (int ii = 0; ii < 5; ++ii) if (tm.valid(m)) {
                 const float *fr = X(ii) + tm.ci(m), *wl = X(5 + ii) + tm.ci(m);
                 const float f0 = fr[0];
                 const float dfr = M::slope(M::sub(fr[1], f0), M::sub(f0, fr[-1]));
@@ -335,6 +339,13 @@ fluidx_kernel(FluidxArgs a)
                 if (on[h]) g[lane + 32 * h] = US[off[h] + i * 5];
         }
     }
+}
+
+template <int CPL, int WPP, class M, bool ROWS, int NT>
+__global__ void __launch_bounds__(256)
+fluidx_kernel(FluidxArgs a)
+{
+    fluidx_tile<CPL, WPP, M, ROWS, NT>(a, blockIdx.x);
 }
 
 // Launch one instantiation; sets the dynamic shared-memory attribute once per

@@ -72,15 +72,19 @@ def _edge_potential_curl(ax, ay, az):
     return np.stack([bx, by, bz])
 
 
-def alfven_oblique(n=128, kvec=(1, 1, 1), amp=1e-3, rho0=1.0, p0=1.0, dtype=np.float32):
-    """Linear Alfven wave with wave vector k = kvec 2pi/L and B0 = khat.
+def alfven_oblique(n=128, kvec=(1, 1, 1), amp=1e-3, rho0=1.0, p0=1.0, dtype=np.float32,
+                   ny=None, nz=None):
+    """Linear Alfven wave with wave vector k = (kvec_i 2pi/L_i) and B0 = khat.
 
     The perturbation direction is e1 = normalised (khat x z) (or khat x x when
     khat is parallel to z); dv = A cos(k.x) e1 at cell centres and
     dB = -A sqrt(rho) cos(k.x) e1 from a staggered vector potential, so the
-    face field is divergence-free to round-off."""
-    nx = ny = nz = n
-    kv = np.asarray(kvec, dtype=np.float64) * 2 * np.pi / n
+    face field is divergence-free to round-off.  ny, nz default to n (cubic);
+    on a non-cubic box the wave stays periodic (kvec integer per axis)."""
+    nx = n
+    ny = n if ny is None else ny
+    nz = n if nz is None else nz
+    kv = np.asarray(kvec, dtype=np.float64) * 2 * np.pi / np.array([nx, ny, nz], dtype=np.float64)
     kh = kv / np.linalg.norm(kv)
     ref = np.array([0.0, 0.0, 1.0]) if abs(kh[2]) < 0.9 else np.array([1.0, 0.0, 0.0])
     e1 = np.cross(kh, ref)
@@ -101,6 +105,72 @@ def alfven_oblique(n=128, kvec=(1, 1, 1), amp=1e-3, rho0=1.0, p0=1.0, dtype=np.f
     b += kh[:, None, None, None]
     e = _energy(rho, m, b, p0)
     return _pack(rho, m, e, b, dtype)
+
+
+def _spectral_field(r, nx, ny, nz, slope):
+    """Real Gaussian random field on (nz, ny, nx) whose Fourier amplitudes go as
+    |k|^slope (k in units of the longest axis' fundamental; no k = 0 mode)."""
+    lmax = float(max(nx, ny, nz))
+    kz = np.fft.fftfreq(nz) * nz * (lmax / nz)
+    ky = np.fft.fftfreq(ny) * ny * (lmax / ny)
+    kx = np.fft.rfftfreq(nx) * nx * (lmax / nx)
+    kk = np.sqrt(kz[:, None, None] ** 2 + ky[None, :, None] ** 2 + kx[None, None, :] ** 2)
+    amp = np.zeros_like(kk)
+    amp[kk > 0] = kk[kk > 0] ** slope
+    noise = np.fft.rfftn(r.standard_normal((nz, ny, nx)))
+    return np.fft.irfftn(noise * amp, s=(nz, ny, nx))
+
+
+def turbulence(nx, ny=None, nz=None, seed=0, mach=0.5, b_mean=0.3, db_rms=None, v_rms=None,
+               rho0=1.0, p0=1.0, dtype=np.float32):
+    """Seeded Gaussian-random turbulent start.
+
+    Velocity: each component a Gaussian random field with Fourier amplitudes
+    |k|^-2 (shell energy spectrum E(k) ~ k^-2), scaled to rms |v| = mach * c_s
+    (c_s = sqrt(gamma p0/rho0)) unless v_rms is given.  Field: B = B_mean x +
+    curl A, A a vector potential with Fourier amplitudes |k|^-2.5 (E_A(k) ~
+    k^-3) on the cell edges, so the face field is divergence-free to round-off;
+    the fluctuation is scaled to rms |dB| = db_rms (default: the rms |v|).
+    rho = rho0, p = p0 uniform."""
+    ny = nx if ny is None else ny
+    nz = nx if nz is None else nz
+    r = np.random.default_rng(seed)
+    v = np.stack([_spectral_field(r, nx, ny, nz, -2.0) for _ in range(3)])
+    target_v = mach * np.sqrt(GAMMA * p0 / rho0) if v_rms is None else v_rms
+    v *= target_v / np.sqrt((v ** 2).sum(0).mean())
+    a = [_spectral_field(r, nx, ny, nz, -2.5) for _ in range(3)]
+    db = _edge_potential_curl(*a)
+    target_b = target_v if db_rms is None else db_rms
+    db *= target_b / np.sqrt((db ** 2).sum(0).mean())
+    db[0] += b_mean
+    rho = np.full((nz, ny, nx), rho0)
+    m = rho[None] * v
+    e = _energy(rho, m, db, p0)
+    return _pack(rho, m, e, db, dtype)
+
+
+def ensemble(nbox=64, seed=0, sizes=(32, 48, 64, 96, 128), amp_range=(1e-4, 1e-1),
+             dtype=np.float32):
+    """The batched-ensemble workload: nbox independent periodic boxes whose
+    sizes along each axis are drawn from `sizes` by seed (non-cubic, uneven),
+    each a linear Alfven wave on the box diagonal (kvec = (1,1,1) per axis) or a
+    turbulent start (turbulence(), rms |v| = rms |dB| = the amplitude), with an
+    amplitude drawn log-uniformly from amp_range.
+
+    Returns a list of dicts {dims: (nx, ny, nz), kind, amp, seed, u, b}."""
+    r = np.random.default_rng(seed)
+    out = []
+    for i in range(nbox):
+        dims = tuple(int(x) for x in r.choice(sizes, size=3))
+        amp = float(np.exp(r.uniform(np.log(amp_range[0]), np.log(amp_range[1]))))
+        kind = "alfven" if r.random() < 0.5 else "turbulent"
+        bseed = int(r.integers(0, 2 ** 31 - 1))
+        if kind == "alfven":
+            u, b = alfven_oblique(dims[0], amp=amp, ny=dims[1], nz=dims[2], dtype=dtype)
+        else:
+            u, b = turbulence(*dims, seed=bseed, v_rms=amp, db_rms=amp, dtype=dtype)
+        out.append({"dims": dims, "kind": kind, "amp": amp, "seed": bseed, "u": u, "b": b})
+    return out
 
 
 def random_state(nx, ny, nz, seed=0, dtype=np.float32, amp=0.3, bmean=(0.3, 0.1, -0.2)):

@@ -24,7 +24,9 @@ MHD_CFL_AVERAGED = 1
 MHD_HEALTH_NONFINITE = 1
 MHD_HEALTH_DENSITY = 2
 MHD_HEALTH_PRESSURE = 4
-KCLASS = {"fluidx": 0, "advectbyzx": 1, "transpose": 2, "cfl": 3}
+MHD_HEALTH_STALL = 8
+MHD_BATCH_MAX_PENCIL = 256
+KCLASS = {"fluidx": 0, "advectbyzx": 1, "transpose": 2, "cfl": 3, "batch": 4}
 
 # every symbol the C headers declare
 EXPORTS = [
@@ -37,6 +39,9 @@ EXPORTS = [
     "mhdgpu_run_host", "mhdgpu_set_math", "mhdgpu_set_tile", "mhdgpu_get_tile",
     "mhdgpu_autotune", "mhdgpu_profiler_create", "mhdgpu_profiler_destroy",
     "mhdgpu_profiler_attach", "mhdgpu_profiler_reset", "mhdgpu_profiler_summary",
+    "mhdgpu_batch_workspace_bytes", "mhdgpu_batch_create", "mhdgpu_batch_destroy",
+    "mhdgpu_batch_advance", "mhdgpu_batch_read_clocks", "mhdgpu_batch_set_schedule",
+    "mhdgpu_batch_get_schedule", "mhdgpu_batch_tune",
     # include/mhdgpu_compat.h
     "fluidx", "advectbyzx", "transpose12", "transpose13", "calcfl", "copy_matrix",
     "mhdgpu_compat_status",
@@ -94,6 +99,14 @@ def lib() -> C.CDLL:
             "mhdgpu_profiler_attach": (I, [P]),
             "mhdgpu_profiler_reset": (I, [P]),
             "mhdgpu_profiler_summary": (I, [P, I, P, P, P]),
+            "mhdgpu_batch_workspace_bytes": (S, [I, P]),
+            "mhdgpu_batch_create": (I, [P, I, P, P, P, D, I, P]),
+            "mhdgpu_batch_destroy": (I, [P]),
+            "mhdgpu_batch_advance": (I, [P, I, P]),
+            "mhdgpu_batch_read_clocks": (I, [P, P, P]),
+            "mhdgpu_batch_set_schedule": (I, [P, I, I, I]),
+            "mhdgpu_batch_get_schedule": (I, [P, I, P, P]),
+            "mhdgpu_batch_tune": (I, [P, P]),
             "calcfl": (F, [P, P, P, P, P]),
             "mhdgpu_compat_status": (I, []),
         }
@@ -284,6 +297,68 @@ class Profiler:
     def close(self):
         if self.h:
             lib().mhdgpu_profiler_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def batch_workspace_bytes(dims) -> int:
+    """Device bytes mhdgpu_batch_create allocates for boxes of these sizes (0 if invalid)."""
+    flat = [int(v) for d in dims for v in d]
+    arr = (C.c_int * len(flat))(*flat)
+    return int(lib().mhdgpu_batch_workspace_bytes(len(dims), arr))
+
+
+class Batch:
+    """Batched ensemble (mhdgpu_batch_*): boxes[i] = (u, b, (nx, ny, nz)) with u, b
+    flat float32 CUDA tensors in the reference layout, advanced in place.
+
+    The tensors must outlive the handle; the handle keeps references to them."""
+
+    def __init__(self, boxes, cfl_number=0.7, cfl_mode=MHD_CFL_C, tf=None):
+        self.boxes = list(boxes)
+        n = len(self.boxes)
+        flat = [int(v) for _, _, d in self.boxes for v in d]
+        dims = (C.c_int * len(flat))(*flat)
+        us = (C.c_void_p * n)(*[u.data_ptr() for u, _, _ in self.boxes])
+        bs = (C.c_void_p * n)(*[b.data_ptr() for _, b, _ in self.boxes])
+        tfa = None if tf is None else (C.c_float * n)(*[float(x) for x in tf])
+        self.h = C.c_void_p()
+        _check(lib().mhdgpu_batch_create(C.byref(self.h), n, dims, us, bs, float(cfl_number),
+                                         int(cfl_mode), tfa))
+
+    def advance(self, nsteps=1, stream=None):
+        _check(lib().mhdgpu_batch_advance(self.h, int(nsteps), _stream(stream)))
+
+    def clocks(self, stream=None, check=True):
+        """Synchronises and returns the boxes' Clock records; with check, raises on
+        a stall (MHD_ERR_TIMEOUT) or an unphysical box (MHD_ERR_UNPHYSICAL)."""
+        out = (Clock * len(self.boxes))()
+        st = lib().mhdgpu_batch_read_clocks(self.h, out, _stream(stream))
+        if check:
+            _check(st)
+        return list(out)
+
+    def set_schedule(self, axis, threads, ctas_per_sm):
+        _check(lib().mhdgpu_batch_set_schedule(self.h, int(axis), int(threads), int(ctas_per_sm)))
+
+    def get_schedule(self, axis):
+        t, c = C.c_int(), C.c_int()
+        _check(lib().mhdgpu_batch_get_schedule(self.h, int(axis), C.byref(t), C.byref(c)))
+        return t.value, c.value
+
+    def tune(self, stream=None):
+        """Autotune the block schedule per axis; returns [(threads, ctas_per_sm)] * 3."""
+        _check(lib().mhdgpu_batch_tune(self.h, _stream(stream)))
+        return [self.get_schedule(a) for a in range(3)]
+
+    def close(self):
+        if self.h:
+            lib().mhdgpu_batch_destroy(self.h)
             self.h = C.c_void_p()
 
     def __del__(self):

@@ -99,3 +99,38 @@ def test_workspace_sizes(L):
     assert L.mhdgpu_advectbyzx_scratch_bytes(16, 8, 4) == 8 * 16 * 8 * 4
     assert L.mhdgpu_step_workspace_bytes(0, 1, 1) == 0
     assert L.mhdgpu_step_fused_workspace_bytes(32, 16, 8) == 8 * 32 * 16 * 8
+
+
+def test_batch_arguments_rejected_without_a_gpu(L):
+    import mhdgpu
+    P = C.c_void_p
+    h = P()
+    good = [8, 8, 8, 32, 48, 64]
+    fake = (P * 2)(P(0x1000), P(0x2000))
+    dims = (C.c_int * 6)(*good)
+    # axis outside 1 .. MHD_BATCH_MAX_PENCIL, no boxes, null tables, bad CFL
+    bad = (C.c_int * 6)(8, 8, 8, 32, 257, 64)
+    assert L.mhdgpu_batch_create(C.byref(h), 2, bad, fake, fake, 0.7, 0, None) == mhdgpu.MHD_ERR_ARG
+    assert b"MHD_BATCH_MAX_PENCIL" in L.mhdgpu_last_error()
+    assert L.mhdgpu_batch_create(C.byref(h), 0, dims, fake, fake, 0.7, 0, None) == mhdgpu.MHD_ERR_ARG
+    assert L.mhdgpu_batch_create(C.byref(h), 2, dims, None, fake, 0.7, 0, None) == mhdgpu.MHD_ERR_ARG
+    nulls = (P * 2)(P(0x1000), None)
+    assert L.mhdgpu_batch_create(C.byref(h), 2, dims, fake, nulls, 0.7, 0, None) == mhdgpu.MHD_ERR_ARG
+    assert L.mhdgpu_batch_create(C.byref(h), 2, dims, fake, fake, 0.0, 0, None) == mhdgpu.MHD_ERR_ARG
+    assert L.mhdgpu_batch_create(C.byref(h), 2, dims, fake, fake, 0.7, 7, None) == mhdgpu.MHD_ERR_ARG
+    assert L.mhdgpu_batch_create(None, 2, dims, fake, fake, 0.7, 0, None) == mhdgpu.MHD_ERR_ARG
+    assert not h.value
+    # calls on a null handle
+    assert L.mhdgpu_batch_advance(None, 1, None) == mhdgpu.MHD_ERR_ARG
+    assert L.mhdgpu_batch_set_schedule(None, 0, 128, 2) == mhdgpu.MHD_ERR_ARG
+    assert L.mhdgpu_batch_destroy(None) == mhdgpu.MHD_ERR_ARG
+
+
+def test_batch_workspace_bytes(L):
+    import mhdgpu
+    dims = [(8, 8, 8), (32, 48, 64)]
+    cells = 8 ** 3 + 32 * 48 * 64
+    ws = mhdgpu.batch_workspace_bytes(dims)
+    assert 8 * cells < ws < 8 * cells + 4096
+    assert mhdgpu.batch_workspace_bytes([(8, 8, 0)]) == 0
+    assert mhdgpu.batch_workspace_bytes([(8, 300, 8)]) == 0

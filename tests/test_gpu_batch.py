@@ -1,0 +1,197 @@
+"""GPU tests of the batched ensemble (mhdgpu_batch_*), through the C ABI.
+
+The batch runs each box through the same tile functions and rounding as the
+transpose-free single-box step, so the bar is bit-for-bit equality with
+mhdgpu_advance(path = MHD_PATH_FUSED) run box by box (whose own parity with the
+oracle is covered in test_gpu_parity.py), for the state and for the clocks.
+"""
+import numpy as np
+import pytest
+
+from util import bits_equal
+
+pytestmark = pytest.mark.gpu
+
+# one box per team class of the batched kernel along some axis: n < 32, 32,
+# 33..63, 64, 65..127, 96, 128, 129..256 (x, y or z pencils)
+CLASS_BOXES = [(8, 16, 24), (32, 48, 20), (64, 40, 12), (96, 8, 16), (130, 12, 8), (16, 200, 8),
+               (8, 8, 128), (100, 16, 10), (5, 7, 9), (1, 4, 3)]
+
+
+def dev(a):
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def host(t):
+    import torch
+    torch.cuda.synchronize()
+    return t.cpu().numpy()
+
+
+def _states(dims_list, seed=5, amp=0.2):
+    import ics
+    return [ics.random_state(*d, seed=seed + i, amp=amp) for i, d in enumerate(dims_list)]
+
+
+def _per_box(gpu, states, dims_list, nsteps, cfl, mode=0, tf=None):
+    import torch
+    out = []
+    for i, ((u, b), d) in enumerate(zip(states, dims_list)):
+        du, db = dev(u), dev(b)
+        work = torch.empty(gpu.step_workspace_bytes(*d, gpu.MHD_PATH_FUSED), dtype=torch.uint8, device="cuda")
+        clock = gpu.new_clock()
+        log = torch.zeros(max(nsteps, 1), dtype=torch.float32, device="cuda")
+        gpu.advance(du, db, *d, nsteps, cfl, mode, 0.0 if tf is None else tf[i], clock, log, work,
+                    gpu.MHD_PATH_FUSED)
+        out.append((host(du), host(db), gpu.read_clock(clock)))
+    return out
+
+
+def _batched(gpu, states, dims_list, nsteps, cfl, mode=0, tf=None, schedule=None):
+    boxes = [(dev(u), dev(b), d) for (u, b), d in zip(states, dims_list)]
+    bt = gpu.Batch(boxes, cfl_number=cfl, cfl_mode=mode, tf=tf)
+    if schedule:
+        for axis, (t, c) in enumerate(schedule):
+            bt.set_schedule(axis, t, c)
+    bt.advance(nsteps)
+    clocks = bt.clocks()
+    res = [(host(u), host(b), c) for (u, b, _), c in zip(boxes, clocks)]
+    bt.close()
+    return res
+
+
+def _same(a, b):
+    for (u1, b1, c1), (u2, b2, c2) in zip(a, b):
+        assert bits_equal(u1, u2) and bits_equal(b1, b2)
+        assert (c1.t, c1.dt, c1.iter, c1.health) == (c2.t, c2.dt, c2.iter, c2.health)
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+def test_batch_equals_per_box_fused_bitwise(gpu, mode):
+    """Every team class (all pencil-length classes along x, y and z), both CFL
+    formulas: the batch ends where the boxes advanced one by one end."""
+    states = _states(CLASS_BOXES)
+    ref = _per_box(gpu, states, CLASS_BOXES, 4, 0.7, mode)
+    got = _batched(gpu, states, CLASS_BOXES, 4, 0.7, mode)
+    _same(got, ref)
+    assert all(c.iter == 4 for _, _, c in got)
+
+
+@pytest.mark.parametrize("schedule", [[(256, 1)] * 3, [(128, 2)] * 3, [(128, 4), (256, 2), (128, 1)],
+                                      [(256, 8)] * 3])
+def test_batch_schedules_agree(gpu, schedule):
+    """The block schedule (pencils per CTA, CTAs per SM) changes no value."""
+    dims = CLASS_BOXES
+    states = _states(dims, seed=11)
+    ref = _batched(gpu, states, dims, 2, 0.8)
+    got = _batched(gpu, states, dims, 2, 0.8, schedule=schedule)
+    _same(got, ref)
+
+
+def test_batch_threads64_without_long_pencils(gpu):
+    """64 threads per CTA serve pencils up to 127 cells; longer ones need a
+    128-thread team and the schedule is refused."""
+    dims = [(8, 16, 24), (100, 16, 10), (32, 48, 20)]
+    states = _states(dims, seed=2)
+    ref = _batched(gpu, states, dims, 2, 0.7)
+    got = _batched(gpu, states, dims, 2, 0.7, schedule=[(64, 4)] * 3)
+    _same(got, ref)
+    boxes = [(dev(u), dev(b), d) for (u, b), d in zip(_states([(130, 4, 4)]), [(130, 4, 4)])]
+    bt = gpu.Batch(boxes)
+    with pytest.raises(gpu.MhdError) as ei:
+        bt.set_schedule(0, 64, 2)
+    assert ei.value.status == gpu.MHD_ERR_ARG
+    bt.set_schedule(1, 64, 2)   # y and z pencils are 4 cells long: fine
+    bt.close()
+
+
+def test_batch_tf_clamp_and_stop(gpu):
+    """Per-box end times: dt clamps to (tf - t)/2 and steps after the end are
+    no-ops, as in mhdgpu_advance."""
+    dims = [(16, 16, 16), (24, 8, 12), (32, 12, 8)]
+    states = _states(dims, seed=9, amp=0.1)
+    tf = [0.5, 1.0, 100.0]
+    ref = _per_box(gpu, states, dims, 12, 0.9, tf=tf)
+    got = _batched(gpu, states, dims, 12, 0.9, tf=tf)
+    _same(got, ref)
+    assert abs(got[0][2].t - 0.5) < 1e-6 and got[0][2].iter < 12
+
+
+def test_batch_tune_restores_state(gpu):
+    """The autotuner times schedules on the batch's own boxes and puts the
+    state and clocks back: afterwards the run equals an untuned one."""
+    dims = [(32, 48, 20), (64, 40, 12), (96, 8, 16), (16, 200, 8)]
+    states = _states(dims, seed=3)
+    ref = _batched(gpu, states, dims, 3, 0.7)
+    boxes = [(dev(u), dev(b), d) for (u, b), d in zip(states, dims)]
+    bt = gpu.Batch(boxes, cfl_number=0.7)
+    sched = bt.tune()
+    assert all(t in (64, 128, 256) and 1 <= c <= 4 for t, c in sched)
+    for (u, b, _), (u0, b0) in zip(boxes, states):
+        assert bits_equal(host(u), u0) and bits_equal(host(b), b0)
+    assert all(c.iter == 0 and c.t == 0.0 for c in bt.clocks())
+    bt.advance(3)
+    clocks = bt.clocks()
+    got = [(host(u), host(b), c) for (u, b, _), c in zip(boxes, clocks)]
+    bt.close()
+    _same(got, ref)
+
+
+def test_batch_graph_replay(gpu):
+    """A captured step replays to the same state as eager steps."""
+    import torch
+    dims = [(32, 16, 24), (48, 32, 16), (8, 64, 8)]
+    states = _states(dims, seed=4)
+    ref = _batched(gpu, states, dims, 3, 0.7)
+    boxes = [(dev(u), dev(b), d) for (u, b), d in zip(states, dims)]
+    bt = gpu.Batch(boxes, cfl_number=0.7)
+    s = torch.cuda.Stream()
+    # snapshot, warm the launch path once, restore, then capture one step
+    snap = [(u.clone(), b.clone()) for u, b, _ in boxes]
+    with torch.cuda.stream(s):
+        bt.advance(1)
+    torch.cuda.synchronize()
+    bt.close()
+    for (u, b, _), (u0, b0) in zip(boxes, snap):
+        u.copy_(u0)
+        b.copy_(b0)
+    bt = gpu.Batch(boxes, cfl_number=0.7)
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=s):
+        bt.advance(1, stream=s)
+    for _ in range(3):
+        g.replay()
+    torch.cuda.synchronize()
+    clocks = bt.clocks()
+    got = [(host(u), host(b), c) for (u, b, _), c in zip(boxes, clocks)]
+    bt.close()
+    _same(got, ref)
+
+
+def test_batch_fast_math_equals_per_box(gpu):
+    dims = [(32, 48, 20), (100, 16, 10), (8, 8, 128)]
+    states = _states(dims, seed=8)
+    prev = gpu.set_math(gpu.MHD_MATH_FAST)
+    try:
+        ref = _per_box(gpu, states, dims, 3, 0.7)
+        got = _batched(gpu, states, dims, 3, 0.7)
+    finally:
+        gpu.set_math(prev)
+    _same(got, ref)
+
+
+def test_batch_ensemble_workload_sample(gpu):
+    """Twelve boxes of the ensemble workload (sizes {32,48,64,96,128} by
+    seed, Alfven or turbulent starts): equal to box-by-box runs, finite, with
+    div B held at round-off."""
+    import ics
+    ens = ics.ensemble(12, seed=1, sizes=(32, 48, 64))
+    dims = [e["dims"] for e in ens]
+    states = [(e["u"], e["b"]) for e in ens]
+    ref = _per_box(gpu, states, dims, 5, 0.7)
+    got = _batched(gpu, states, dims, 5, 0.7)
+    _same(got, ref)
+    for (u, b, c), e in zip(got, ens):
+        assert np.isfinite(u).all() and c.health & (gpu.MHD_HEALTH_NONFINITE | gpu.MHD_HEALTH_DENSITY) == 0
+        assert ics.div_b(b, *e["dims"]) < 2 * ics.div_b(e["b"], *e["dims"]) + 1e-6
