@@ -1,23 +1,36 @@
-"""Benchmark of one full MHD step (x, y, z, z, y, x sweeps + CFL) on GB300.
+"""Benchmark of full MHD steps (x, y, z, z, y, x sweeps + CFL) on GB300.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--n 128]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload ensemble64|alfven_diag_128]
 
-Workload: the 128^3 configuration of the reference's plain drop-in case, a
-linear Alfven wave on the box diagonal k = (1,1,1) 2 pi/L, A = 1e-3, rho = p = 1,
-CFL 0.7 (C-path CFL formula), synthetic inputs (mhd-gpu_gb300/ics.py).
-A step is one full Strang-split step; one cell-update is one cell advanced by
-one step.  value = cell-updates/s over K steps replayed from a CUDA graph with
-the state resident in HBM; L2 is flushed (512 MB write) between timed steps,
-outside the timed events.  e2e = the same metric through the host-buffer C-ABI
-entry mhdgpu_run_host (pinned host state uploaded and downloaded every step).
+Workloads (synthetic inputs, mhd-gpu_gb300/ics.py):
+  ensemble64 (default, the headline "fused+batched vs plain"): 64 independent
+    periodic boxes, sizes along each axis drawn from {32,48,64,96,128} by seed 0
+    (27.2 M cells, 0.87 GB of state), each a linear Alfven wave on the box
+    diagonal or a turbulent start with an amplitude drawn log-uniformly from
+    [1e-4, 1e-1]; CFL 0.7, C-path CFL formula.  The batched path
+    (mhdgpu_batch_*) advances all boxes with one persistent launch per sweep;
+    the comparison loops the plain per-subroutine drop-in (mhdgpu_advance,
+    path PLAIN) box by box, and the fused single-box step box by box.
+  alfven_diag_128: the 128^3 plain drop-in configuration, a linear Alfven wave
+    on the box diagonal k = (1,1,1) 2 pi/L, A = 1e-3, rho = p = 1, CFL 0.7.
+    Its numbers are also reported inside the ensemble line.
 
-With N > 1 (torchrun) every rank advances its own replica of the box: the
-single-box step has no data-parallel split, so scaling is weak and the ranks
-exchange nothing but the timing max.
+A step is one full Strang-split step of every box; one cell-update is one
+cell advanced by one step.  value = cell-updates/s over K steps replayed from
+a CUDA graph with the state resident in HBM; L2 is flushed (512 MB write)
+between timed steps, outside the timed events (the ensemble's state is also
+larger than L2).  e2e = the same metric through the public API with host
+buffers: every step uploads the state from pinned host memory, advances one
+step and downloads it.
+
+With N > 1 (torchrun) every rank advances its own replica of the workload:
+nothing is exchanged but the timing max, so scaling is weak.
 
 --impl reference times the reference algorithm's CPU implementation on this
 host's cores (the C restatement in oracle/, OpenMP over pencils, bit-identical
-to the reference C path) on the same workload and prints the same JSON line.
+to the reference C path) on a bounded sample of the same workload and prints
+the same JSON line.
 """
 from __future__ import annotations
 
@@ -37,8 +50,13 @@ sys.path.insert(0, os.path.join(REPO, "oracle"))
 METRIC = "cell-updates/s per full MHD step, fused+batched vs plain; % of HBM roofline"
 UNIT = "cell-updates/s"
 FLUIDX_BYTES_PER_CELL = 52      # R u 20 + b 12, W u 20 (one read and write of the pencil data)
+# one sweep of the batched kernel per cell: fluid 52 (above); field 32 (R rho, m 8,
+# R b2 b3 8, W b2 b3 8, W sA sB 8); b(1) 16 (R sA sB 8, R+W b1 8)
+SWEEP_BYTES_PER_CELL = 100
 STEP_BYTES_64 = 64              # one read + one write of the 8-float state per cell-update
 PLAIN_PASS_BYTES = 792          # minimal per-subroutine pass bytes per cell-update
+ENSEMBLE = {"nbox": 64, "seed": 0, "sizes": (32, 48, 64, 96, 128), "amp_range": (1e-4, 1e-1)}
+CFL = 0.7
 
 
 def peaks():
@@ -60,7 +78,6 @@ class ClockSampler:
         self.samples = []
         self.proc = None
         self.thread = None
-        self.marks = []
 
     def start(self):
         try:
@@ -77,9 +94,6 @@ class ClockSampler:
     def _read(self):
         for line in self.proc.stdout:
             self.samples.append((time.time(), line.strip()))
-
-    def mark(self, name):
-        self.marks.append((name, time.time()))
 
     def stop(self):
         if self.proc:
@@ -113,9 +127,9 @@ class ClockSampler:
                 "samples": len(inside)}
 
 
-def read_traffic():
-    """dram bytes per fluidx launch from the committed ncu summary, if any."""
-    p = os.path.join(REPO, "profiles", "fluidx_alfven128_ncu.txt")
+def read_traffic(name):
+    """dram bytes per launch of a kernel from its committed ncu summary, if any."""
+    p = os.path.join(REPO, "profiles", name)
     if not os.path.exists(p):
         return None
     for line in open(p):
@@ -157,37 +171,273 @@ def dist_barrier(world):
         dist.barrier()
 
 
+# ---------------------------------------------------------------- CPU arms
+def _cpu_path(threads, use_ref):
+    import oracle as O
+    if use_ref:
+        return O.reference("f32"), "reference", 1
+    O.set_threads(threads)
+    return O.oracle("f32"), "port", threads
+
+
 def cpu_rate(n, seconds, threads, use_ref):
     """Cell-updates/s of the reference algorithm on the host: whole steps of the
-    same workload until `seconds` of work have run (at least one step)."""
+    n^3 Alfven workload until `seconds` of work have run (at least one step)."""
     import numpy as np
     import ics
-    import oracle as O
     u, b = ics.alfven_oblique(n)
-    if use_ref:
-        P = O.reference("f32")
-        kind = "reference"
-        threads = 1
-    else:
-        O.set_threads(threads)
-        P = O.oracle("f32")
-        kind = "port"
-    # one untimed step to page everything in
-    inv = P.calcfl(u, b, n, n, n)
-    dt = P.dt_from_cfl(inv, 0.7, np.float32(0), np.float32(0))
-    P.step(u, b, n, n, n, dt)
+    P, kind, threads = _cpu_path(threads, use_ref)
+    inv = P.calcfl(u, b, n, n, n)      # one untimed step pages everything in
+    P.step(u, b, n, n, n, P.dt_from_cfl(inv, CFL, np.float32(0), np.float32(0)))
     steps = 0
     t0 = time.perf_counter()
     while True:
         inv = P.calcfl(u, b, n, n, n)
-        dt = P.dt_from_cfl(inv, 0.7, np.float32(0), np.float32(0))
-        P.step(u, b, n, n, n, dt)
+        P.step(u, b, n, n, n, P.dt_from_cfl(inv, CFL, np.float32(0), np.float32(0)))
         steps += 1
         el = time.perf_counter() - t0
         if el >= seconds:
             break
-    rate = n ** 3 * steps / el
-    return rate, kind, threads, f"{steps} full steps of the {n}^3 workload ({el:.1f} s)"
+    return n ** 3 * steps / el, kind, threads, f"{steps} full steps of the {n}^3 workload ({el:.1f} s)"
+
+
+def cpu_rate_ensemble(ens, seconds, threads):
+    """Cell-updates/s of the oracle port on the ensemble: full steps of its
+    boxes in order (wrapping around) until `seconds` of work have run.  The
+    reference's own C path cannot run these boxes (its transpose13 refuses
+    nx != nz, Heterogeneous_MHD/C/transpose13.c:58-61), so this is the port."""
+    import numpy as np
+    P, kind, threads = _cpu_path(threads, False)
+    states = [(e["u"].copy(), e["b"].copy(), e["dims"]) for e in ens]
+    u, b, d = states[0]
+    P.step(u, b, *d, P.dt_from_cfl(P.calcfl(u, b, *d), CFL, np.float32(0), np.float32(0)))
+    cells = steps = 0
+    t0 = time.perf_counter()
+    i = 0
+    while True:
+        u, b, d = states[i % len(states)]
+        P.step(u, b, *d, P.dt_from_cfl(P.calcfl(u, b, *d), CFL, np.float32(0), np.float32(0)))
+        cells += d[0] * d[1] * d[2]
+        steps += 1
+        i += 1
+        el = time.perf_counter() - t0
+        if el >= seconds:
+            break
+    return cells / el, kind, threads, (f"{steps} box-steps of the ensemble's boxes in order "
+                                       f"({cells / 1e6:.1f} M cell-updates, {el:.1f} s)")
+
+
+# ---------------------------------------------------------------- GPU timing
+def timed_replays(graph_fn, K, W, stream, flush, world):
+    """K graph replays bracketed by CUDA events on `stream`, L2 flushed before
+    each (outside the events), after W untimed replays; returns (seconds, wall)."""
+    import torch
+    with torch.cuda.stream(stream):
+        for _ in range(W):
+            flush.zero_()
+            graph_fn()
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
+    dist_barrier(world)
+    torch.cuda.synchronize()
+    tw0 = time.time()
+    with torch.cuda.stream(stream):
+        for i in range(K):
+            flush.zero_()
+            ev[i][0].record(stream)
+            graph_fn()
+            ev[i][1].record(stream)
+    torch.cuda.synchronize()
+    tw1 = time.time()
+    dist_barrier(world)
+    return dist_max(sum(a.elapsed_time(b) for a, b in ev) / 1e3, world), (tw0, tw1)
+
+
+def capture(fn, stream, warm=2):
+    import torch
+    with torch.cuda.stream(stream):          # sets kernel attributes before capture
+        for _ in range(warm):
+            fn()
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=stream):
+        fn()
+    torch.cuda.synchronize()
+    return g
+
+
+def profiled(fn, steps, stream, flush):
+    import torch
+    import mhdgpu
+    prof = mhdgpu.Profiler(max_records=steps * 2000 + 100)
+    with torch.cuda.stream(stream):
+        with prof:
+            for _ in range(steps):
+                flush.zero_()
+                fn()
+    torch.cuda.synchronize()
+    s = prof.summary()
+    prof.close()
+    return s
+
+
+def single_box(n, K, W, stream, flush, world, dev, tune, math_mode):
+    """The 128^3 (n^3) single-box numbers: fused and plain steps, the fluidx
+    roofline and the e2e host-buffer call."""
+    import torch
+    import ics
+    import mhdgpu
+    ncell = n ** 3
+    if tune:
+        picks = mhdgpu.autotune(n, n, n, math_mode)
+    else:
+        picks = {(k, n, r): mhdgpu.get_tile(k, n, rows=r) for k in ("fluidx", "advectbyzx")
+                 for r in (False, True)}
+    u0, b0 = ics.alfven_oblique(n)
+    res = {"workload": f"alfven_diag_{n}", "box": [n, n, n],
+           "tiles": {f"{k}@{m}{'/rows' if r else ''}": list(v) for (k, m, r), v in picks.items()},
+           "tiles_from": "mhdgpu_autotune" if tune else "defaults"}
+    for path, name in ((mhdgpu.MHD_PATH_FUSED, "fused"), (mhdgpu.MHD_PATH_PLAIN, "plain")):
+        du = torch.from_numpy(u0).to(dev)
+        db = torch.from_numpy(b0).to(dev)
+        work = torch.empty(mhdgpu.step_workspace_bytes(n, n, n, path), dtype=torch.uint8, device=dev)
+        clock = mhdgpu.new_clock(device=dev)
+
+        def one_step():
+            mhdgpu.advance(du, db, n, n, n, 1, CFL, mhdgpu.MHD_CFL_C, 0.0, clock, None, work, path)
+
+        g = capture(one_step, stream, W)
+        secs, wall = timed_replays(g.replay, K, 1, stream, flush, world)
+        summ = profiled(one_step, K, stream, flush)
+        del g
+        res[name] = {"value": world * ncell * K / secs, "ms_per_step": secs / K * 1e3,
+                     "kernel_time_ms_per_step": {k: v[2] / K for k, v in summ.items()},
+                     "kernel_launches_per_step": {k: v[1] / K for k, v in summ.items()},
+                     "health": mhdgpu.read_clock(clock).health,
+                     "path": "transpose-free step (mhdgpu_step_fused)" if name == "fused"
+                     else "per-subroutine kernels + transposes (mhdgpu_step)"}
+        if name == "fused":
+            fl_rec, fl_launch, fl_ms = summ["fluidx"]
+            fl_avg_s = fl_ms / 1e3 / max(fl_launch, 1)
+            hbm, kind = peaks()
+            ach = FLUIDX_BYTES_PER_CELL * ncell / fl_avg_s / 1e9
+            tot_ms = sum(v[2] for v in summ.values())
+            res["fluidx_roofline"] = {
+                "bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
+                "peak_source": f"{kind} (MEASURED_PEAKS.json hbm_gbs)",
+                "traffic": read_traffic("fluidx_alfven128_ncu.txt"),
+                "algorithmic_bytes_per_launch": FLUIDX_BYTES_PER_CELL * ncell,
+                "avg_launch_us": fl_avg_s * 1e6, "share_of_step": fl_ms / tot_ms if tot_ms else None}
+    res["fused_over_plain"] = res["fused"]["value"] / res["plain"]["value"]
+    # end to end through the host-buffer entry (upload, one step, download per call)
+    hu = torch.from_numpy(u0.copy()).pin_memory()
+    hb = torch.from_numpy(b0.copy()).pin_memory()
+    un, bn = hu.numpy(), hb.numpy()
+    ke = max(3, min(K, 50))
+    t = 0.0
+    mhdgpu.run_host(un, bn, n, n, n, CFL, 0, t, 0.0, 1, path=mhdgpu.MHD_PATH_FUSED)
+    dist_barrier(world)
+    t0 = time.perf_counter()
+    for _ in range(ke):
+        _st, t, _d = mhdgpu.run_host(un, bn, n, n, n, CFL, 0, t, 0.0, 1, path=mhdgpu.MHD_PATH_FUSED)
+    secs = dist_max(time.perf_counter() - t0, world)
+    res["e2e"] = {"value": world * ncell * ke / secs, "unit": UNIT, "steps": ke,
+                  "h2d_bytes_per_step": 32 * ncell, "d2h_bytes_per_step": 32 * ncell,
+                  "api": "mhdgpu_run_host, 1 step per call"}
+    return res
+
+
+def ensemble_bench(ens, K, W, stream, flush, world, dev, tune, sampler):
+    """Batched ensemble vs box-by-box loops; e2e through mhdgpu_batch_* with
+    the state uploaded from and downloaded to pinned host memory every step."""
+    import numpy as np
+    import torch
+    import mhdgpu
+    dims = [e["dims"] for e in ens]
+    cells = int(sum(int(np.prod(d)) for d in dims))
+    boxes = [(torch.from_numpy(e["u"]).to(dev), torch.from_numpy(e["b"]).to(dev), e["dims"]) for e in ens]
+    bt = mhdgpu.Batch(boxes, cfl_number=CFL, cfl_mode=mhdgpu.MHD_CFL_C)
+    sched = bt.tune(stream=stream) if tune else [bt.get_schedule(a) for a in range(3)]
+
+    def step():
+        bt.advance(1, stream=stream)
+
+    g = capture(step, stream, 2)
+    t_w0 = time.time()
+    secs, wall = timed_replays(g.replay, K, W, stream, flush, world)
+    del g
+    summ = profiled(step, max(3, min(K, 20)), stream, flush)
+    ksteps = max(3, min(K, 20))
+    clocks = bt.clocks(stream=None, check=False)
+    health = 0
+    for c in clocks:
+        health |= c.health
+    value = world * cells * K / secs
+    b_rec, b_launch, b_ms = summ["batch"]
+    avg_s = b_ms / 1e3 / max(b_launch, 1)
+    hbm, kind = peaks()
+    ach = SWEEP_BYTES_PER_CELL * cells / avg_s / 1e9
+    tot_ms = sum(v[2] for v in summ.values())
+    res = {"value": value, "ms_per_step": secs / K * 1e3, "cells": cells, "schedule": sched,
+           "schedule_from": "mhdgpu_batch_tune" if tune else "defaults", "wall": wall,
+           "kernel_time_ms_per_step": {k: v[2] / ksteps for k, v in summ.items()},
+           "kernel_launches_per_step": {k: v[1] / ksteps for k, v in summ.items()},
+           "health": health,
+           "roofline": {"bound": "hbm",
+                        "kernel": "batch_sweep_kernel (one persistent launch per sweep, all boxes)",
+                        "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
+                        "peak_source": f"{kind} (MEASURED_PEAKS.json hbm_gbs)",
+                        "traffic": read_traffic("batch_sweep_ensemble64_ncu.txt"),
+                        "algorithmic_bytes_per_launch": SWEEP_BYTES_PER_CELL * cells,
+                        "avg_launch_us": avg_s * 1e6,
+                        "share_of_step": b_ms / tot_ms if tot_ms else None}}
+    # box by box: the fused single-box step and the plain per-subroutine drop-in,
+    # each one CUDA graph holding the loop over the 64 boxes
+    kb = max(3, min(K, 30))
+    for path, name in ((mhdgpu.MHD_PATH_FUSED, "boxwise_fused"), (mhdgpu.MHD_PATH_PLAIN, "boxwise_plain")):
+        works = [torch.empty(mhdgpu.step_workspace_bytes(*d, path), dtype=torch.uint8, device=dev) for d in dims]
+        cks = [mhdgpu.new_clock(device=dev) for _ in dims]
+
+        def loop():
+            for (u, b, d), w, c in zip(boxes, works, cks):
+                mhdgpu.advance(u, b, *d, 1, CFL, mhdgpu.MHD_CFL_C, 0.0, c, None, w, path, stream=stream)
+
+        gl = capture(loop, stream, 1)
+        s2, _ = timed_replays(gl.replay, kb, 1, stream, flush, world)
+        del gl
+        res[name] = {"value": world * cells * kb / s2, "ms_per_step": s2 / kb * 1e3, "steps": kb,
+                     "path": ("mhdgpu_advance path FUSED" if path else "mhdgpu_advance path PLAIN (per-subroutine drop-in)")
+                     + " looped over the boxes, one CUDA graph per step"}
+        del works
+    res["batched_over_boxwise_plain"] = value / res["boxwise_plain"]["value"]
+    res["batched_over_boxwise_fused"] = value / res["boxwise_fused"]["value"]
+    # e2e: pinned host state, upload all boxes, one batched step, download all boxes
+    hu = [torch.from_numpy(e["u"].copy()).pin_memory() for e in ens]
+    hb = [torch.from_numpy(e["b"].copy()).pin_memory() for e in ens]
+    ke = max(3, min(K, 20))
+
+    def e2e_step():
+        with torch.cuda.stream(stream):
+            for (u, b, _), x, y in zip(boxes, hu, hb):
+                u.copy_(x, non_blocking=True)
+                b.copy_(y, non_blocking=True)
+            bt.advance(1, stream=stream)
+            for (u, b, _), x, y in zip(boxes, hu, hb):
+                x.copy_(u, non_blocking=True)
+                y.copy_(b, non_blocking=True)
+        stream.synchronize()
+
+    e2e_step()
+    dist_barrier(world)
+    t0 = time.perf_counter()
+    for _ in range(ke):
+        e2e_step()
+    s3 = dist_max(time.perf_counter() - t0, world)
+    res["e2e"] = {"value": world * cells * ke / s3, "unit": UNIT, "steps": ke,
+                  "h2d_bytes_per_step": 32 * cells, "d2h_bytes_per_step": 32 * cells,
+                  "api": "mhdgpu_batch_advance (1 step) between pinned host<->device copies of every box"}
+    bt.close()
+    return res
 
 
 def main():
@@ -196,42 +446,58 @@ def main():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--n", type=int, default=128)
+    ap.add_argument("--workload", default="ensemble64", choices=["ensemble64", "alfven_diag_128"])
+    ap.add_argument("--n", type=int, default=128, help="box size of the single-box workload")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--math", default="faithful", choices=["faithful", "fast"])
-    ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (default tiles)")
+    ap.add_argument("--no-tune", action="store_true", help="skip the autotuners (default tiles)")
     args = ap.parse_args()
     n, K, W = args.n, args.steps, max(3, args.warmup)
-    ncell = n ** 3
-    config = {"workload": f"alfven_diag_{n}", "box": [n, n, n], "cfl": 0.7, "cfl_mode": "c_path",
-              "ic": "linear Alfven wave, k=(1,1,1)2pi/L, A=1e-3, rho=p=1, B0 along k",
-              "path": "plain drop-in: per-subroutine kernels, one CUDA graph per step",
-              "l2": "flushed between timed steps (512 MB write, outside the timed events)",
-              "parallelism": f"replicas x{args.gpus}"}
+    ens_mode = args.workload == "ensemble64"
+    if ens_mode:
+        config = {"workload": "ensemble64", "boxes": ENSEMBLE["nbox"], "sizes": list(ENSEMBLE["sizes"]),
+                  "seed": ENSEMBLE["seed"], "amp_range": list(ENSEMBLE["amp_range"]),
+                  "ic": "per box: linear Alfven wave on the box diagonal or turbulent start "
+                        "(k^-2 velocity, k^-3 vector potential), amplitude log-uniform in [1e-4,1e-1]",
+                  "cfl": CFL, "cfl_mode": "c_path",
+                  "path": "batched: one persistent launch per sweep over all boxes, one CUDA graph per step",
+                  "l2": "flushed between timed steps (512 MB write, outside the timed events); state 0.87 GB > L2",
+                  "parallelism": f"replicas x{args.gpus}"}
+    else:
+        config = {"workload": f"alfven_diag_{n}", "box": [n, n, n], "cfl": CFL, "cfl_mode": "c_path",
+                  "ic": "linear Alfven wave, k=(1,1,1)2pi/L, A=1e-3, rho=p=1, B0 along k",
+                  "path": "transpose-free step (mhdgpu_step_fused), one CUDA graph per step",
+                  "l2": "flushed between timed steps (512 MB write, outside the timed events)",
+                  "parallelism": f"replicas x{args.gpus}"}
 
     if args.impl == "reference":
         rank = int(os.environ.get("RANK", "0"))
         if rank != 0:
             return
         threads = os.cpu_count() or 1
-        use_ref = os.path.exists(os.path.join(REPO, "oracle", "_ref", "libref_f32.so"))
         if not os.path.exists(os.path.join(REPO, "oracle", "lib", "liboracle.so")):
             subprocess.run(["make", "-s", "-C", os.path.join(REPO, "oracle")], check=True)
         budget = min(120.0, max(10.0, 0.25 * (K + W)))
-        rate, kind, cores, sample = cpu_rate(n, budget, threads, use_ref)
+        if ens_mode:
+            import ics
+            ens = ics.ensemble(**ENSEMBLE)
+            rate, kind, cores, sample = cpu_rate_ensemble(ens, budget, threads)
+            ms = sum(e["dims"][0] * e["dims"][1] * e["dims"][2] for e in ens) / rate * 1e3
+        else:
+            use_ref = os.path.exists(os.path.join(REPO, "oracle", "_ref", "libref_f32.so"))
+            rate, kind, cores, sample = cpu_rate(n, budget, threads, use_ref)
+            ms = n ** 3 / rate * 1e3
         print(json.dumps({
             "metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": args.gpus, "steps": K,
-            "warmup": W, "ms_per_step": ncell / rate * 1e3, "higher_is_better": True,
+            "warmup": W, "ms_per_step": ms, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": config, "impl": "reference",
-            "cpu_baseline": {"value": rate, "unit": UNIT, "cores": cores, "kind": kind,
-                             "sample": sample},
+            "cpu_baseline": {"value": rate, "unit": UNIT, "cores": cores, "kind": kind, "sample": sample},
             "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         }))
         return
 
-    import numpy as np
     import torch
 
     import ics
@@ -241,135 +507,67 @@ def main():
     dev = torch.device("cuda", local if world > 1 else 0)
     math_mode = mhdgpu.MHD_MATH_FAST if args.math == "fast" else mhdgpu.MHD_MATH_FAITHFUL
     mhdgpu.set_math(math_mode)
-    if not args.no_tune:
-        picks = mhdgpu.autotune(n, n, n, math_mode)
-    else:
-        picks = {(k, n, r): mhdgpu.get_tile(k, n, rows=r) for k in ("fluidx", "advectbyzx")
-                 for r in (False, True)}
     config["math"] = args.math
-    config["tiles"] = {f"{k}@{m}{'/rows' if r else ''}": list(v) for (k, m, r), v in picks.items()}
-    config["tiles_from"] = "defaults" if args.no_tune else "mhdgpu_autotune"
-    u0, b0 = ics.alfven_oblique(n)
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
     stream = torch.cuda.Stream(device=dev)
     vis = [x.strip() for x in os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",") if x.strip()]
     sampler = ClockSampler(vis[local] if len(vis) > local else local)
     sampler.start()
     time.sleep(0.3)
+    tune = not args.no_tune
 
-    def measure(path):
-        """K graph-replayed steps (L2 flushed between them, outside the
-        events), then K directly launched steps under the event profiler."""
-        du = torch.from_numpy(u0).to(dev)
-        db = torch.from_numpy(b0).to(dev)
-        work = torch.empty(mhdgpu.step_workspace_bytes(n, n, n, path), dtype=torch.uint8, device=dev)
-        clock = mhdgpu.new_clock(device=dev)
-
-        def one_step():
-            mhdgpu.advance(du, db, n, n, n, 1, 0.7, mhdgpu.MHD_CFL_C, 0.0, clock, None, work, path)
-
-        with torch.cuda.stream(stream):          # warm-up; sets kernel attributes before capture
-            for _ in range(W):
-                one_step()
-        torch.cuda.synchronize()
-        graph = torch.cuda.CUDAGraph()
-        with torch.cuda.graph(graph, stream=stream):
-            one_step()
-        torch.cuda.synchronize()
-        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
-        dist_barrier(world)
-        torch.cuda.synchronize()
-        tw0 = time.time()
-        with torch.cuda.stream(stream):
-            for i in range(K):
-                flush.zero_()
-                ev[i][0].record(stream)
-                graph.replay()
-                ev[i][1].record(stream)
-        torch.cuda.synchronize()
-        tw1 = time.time()
-        dist_barrier(world)
-        total_s = dist_max(sum(a.elapsed_time(b) for a, b in ev) / 1e3, world)
-        prof = mhdgpu.Profiler(max_records=K * 40 + 100)
-        with torch.cuda.stream(stream):
-            with prof:
-                for i in range(K):
-                    flush.zero_()
-                    one_step()
-        torch.cuda.synchronize()
-        summ = prof.summary()
-        prof.close()
-        health = mhdgpu.read_clock(clock).health
-        del graph
-        return total_s, summ, health, (tw0, tw1)
-
-    total_s, summ, health, (t_wall0, t_wall1) = measure(mhdgpu.MHD_PATH_FUSED)
-    value = world * ncell * K / total_s
-    plain_s, plain_summ, plain_health, _ = measure(mhdgpu.MHD_PATH_PLAIN)
-    value_plain = world * ncell * K / plain_s
-    sampler.stop()
-    clocks = sampler.summary(t_wall0, t_wall1)
-    launches_per_step = sum(v[1] for v in summ.values()) / K
-    tot_ms = sum(v[2] for v in summ.values())
-    fl_rec, fl_launch, fl_ms = summ["fluidx"]
-    fl_avg_s = fl_ms / 1e3 / max(fl_launch, 1)
-    hbm, peak_kind = peaks()
-    achieved = FLUIDX_BYTES_PER_CELL * ncell / fl_avg_s / 1e9
-    traffic = read_traffic()
-
-    # end to end through the host-buffer C-ABI entry: every step uploads the
-    # state from pinned memory, advances one step and downloads it
-    hu = torch.from_numpy(u0.copy()).pin_memory()
-    hb = torch.from_numpy(b0.copy()).pin_memory()
-    un, bn = hu.numpy(), hb.numpy()
-    ke = max(3, min(K, 50))
-    t = 0.0
-    mhdgpu.run_host(un, bn, n, n, n, 0.7, 0, t, 0.0, 1, path=mhdgpu.MHD_PATH_FUSED)
-    dist_barrier(world)
-    t0 = time.perf_counter()
-    for _ in range(ke):
-        st, t, _done = mhdgpu.run_host(un, bn, n, n, n, 0.7, 0, t, 0.0, 1, path=mhdgpu.MHD_PATH_FUSED)
-    e2e_s = dist_max(time.perf_counter() - t0, world)
-    e2e = world * ncell * ke / e2e_s
-    config["path"] = "transpose-free step (mhdgpu_step_fused), one CUDA graph per step"
-
-    out = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
-        "ms_per_step": total_s / K * 1e3, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic (seedless analytic initial state, see config.ic)",
-        "config": config,
-        "gpu_launches": int(round(launches_per_step * K)),
-        "roofline": {"bound": "hbm",
-                     "kernel": "fluidx_kernel (x sweep %s, y/z sweeps %s [cpl,wpp,ppc], %s)" % (
-                         list(mhdgpu.get_tile("fluidx", n)), list(mhdgpu.get_tile("fluidx", n, rows=True)),
-                         args.math),
-                     "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                     "frac": achieved / hbm, "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
-                     "traffic": traffic,
-                     "algorithmic_bytes_per_launch": FLUIDX_BYTES_PER_CELL * ncell,
-                     "avg_launch_us": fl_avg_s * 1e6,
-                     "share_of_step": fl_ms / tot_ms if tot_ms else None},
-        "roofline_step": {"bytes_per_cell_update_64B_basis": STEP_BYTES_64,
-                          "frac_64B_basis": value * STEP_BYTES_64 / 1e9 / world / hbm,
-                          "plain_pass_bytes_per_cell_update": PLAIN_PASS_BYTES,
-                          "frac_plain_pass_bytes": value * PLAIN_PASS_BYTES / 1e9 / world / hbm},
-        "kernel_time_ms_per_step": {k: v[2] / K for k, v in summ.items()},
-        "kernel_launches_per_step": {k: v[1] / K for k, v in summ.items()},
-        "plain_drop_in": {"value": value_plain, "unit": UNIT, "ms_per_step": plain_s / K * 1e3,
-                          "path": "per-subroutine kernels + transposes (mhdgpu_step)",
-                          "kernel_time_ms_per_step": {k: v[2] / K for k, v in plain_summ.items()},
-                          "health": plain_health},
-        "fused_over_plain": value / value_plain,
-        "e2e": {"value": e2e, "unit": UNIT, "steps": ke,
-                "h2d_bytes_per_step": 32 * ncell, "d2h_bytes_per_step": 32 * ncell,
-                "api": "mhdgpu_run_host, 1 step per call"},
-        "clocks": clocks, "health": health,
-    }
+    sb = single_box(n, K, W, stream, flush, world, dev, tune, math_mode)
+    if ens_mode:
+        ens = ics.ensemble(**ENSEMBLE)
+        eb = ensemble_bench(ens, K, W, stream, flush, world, dev, tune, sampler)
+        sampler.stop()
+        clocks = sampler.summary(*eb["wall"])
+        value, ms_step = eb["value"], eb["ms_per_step"]
+        launches = eb["kernel_launches_per_step"]
+        out_roof = eb["roofline"]
+        out = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
+            "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic (seeded ensemble, see config)", "config": config,
+            "gpu_launches": int(round(sum(launches.values()) * K)),
+            "roofline": out_roof,
+            "roofline_step": {"bytes_per_cell_update_64B_basis": STEP_BYTES_64,
+                              "frac_64B_basis": value * STEP_BYTES_64 / 1e9 / world / out_roof["peak"]},
+            "plain_drop_in": {"value": eb["boxwise_plain"]["value"], "unit": UNIT,
+                              "ms_per_step": eb["boxwise_plain"]["ms_per_step"],
+                              "path": eb["boxwise_plain"]["path"]},
+            "fused_over_plain": eb["batched_over_boxwise_plain"],
+            "ensemble": {k: v for k, v in eb.items() if k not in ("roofline", "wall", "e2e")},
+            "alfven_diag_128": sb,
+            "e2e": eb["e2e"], "clocks": clocks, "health": eb["health"],
+        }
+    else:
+        sampler.stop()
+        fused = sb["fused"]
+        clocks = sampler.summary(0, time.time())
+        out = {
+            "metric": METRIC, "value": fused["value"], "unit": UNIT, "n_gpus": world, "steps": K,
+            "warmup": W, "ms_per_step": fused["ms_per_step"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seedless analytic initial state, see config.ic)", "config": config,
+            "gpu_launches": int(round(sum(fused["kernel_launches_per_step"].values()) * K)),
+            "roofline": sb["fluidx_roofline"],
+            "roofline_step": {"bytes_per_cell_update_64B_basis": STEP_BYTES_64,
+                              "frac_64B_basis": fused["value"] * STEP_BYTES_64 / 1e9 / world
+                              / sb["fluidx_roofline"]["peak"],
+                              "plain_pass_bytes_per_cell_update": PLAIN_PASS_BYTES},
+            "plain_drop_in": {"value": sb["plain"]["value"], "unit": UNIT,
+                              "ms_per_step": sb["plain"]["ms_per_step"], "path": sb["plain"]["path"]},
+            "fused_over_plain": sb["fused_over_plain"],
+            "alfven_diag_128": sb, "e2e": sb["e2e"], "clocks": clocks, "health": fused["health"],
+        }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        use_ref = os.path.exists(os.path.join(REPO, "oracle", "_ref", "libref_f32.so"))
         try:
-            rate, kind, cores, sample = cpu_rate(n, args.cpu_seconds, os.cpu_count() or 1, use_ref)
+            if ens_mode:
+                rate, kind, cores, sample = cpu_rate_ensemble(ens, args.cpu_seconds, os.cpu_count() or 1)
+            else:
+                use_ref = os.path.exists(os.path.join(REPO, "oracle", "_ref", "libref_f32.so"))
+                rate, kind, cores, sample = cpu_rate(n, args.cpu_seconds, os.cpu_count() or 1, use_ref)
             out["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": cores, "kind": kind,
                                    "sample": sample}
         except Exception as e:  # noqa: BLE001

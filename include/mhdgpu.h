@@ -203,6 +203,13 @@ int mhdgpu_run_host(float *u, float *b, int nx, int ny, int nz, double cfl_numbe
 #define MHD_MATH_FAST       1   /* plain FP32 with FMA contraction, hardware
                                    reciprocal and root: faster, ~1 ulp per op
                                    further from the reference */
+#define MHD_MATH_FP64P      2   /* faithful, except that the gas pressure of
+                                   low-beta cells (beta = 2p/B^2 < 0.1 in FP32,
+                                   or p <= 0) is recovered in FP64:
+                                   p = (gamma-1)(E - m^2/2rho - B^2/2) from the
+                                   float state in double (the reference forms
+                                   ps first and p = ps - B^2/2, which cancels
+                                   at low beta, C/mhdflux.c:26-42) */
 
 /* selects the policy of the fluid kernels; returns the previous one */
 int mhdgpu_set_math(int mode);
@@ -224,6 +231,43 @@ int mhdgpu_get_tile(int kclass, int n, int *cpl, int *wpp, int *ppc);
  * mhdgpu_set_tile and returns.  Allocates and frees its own test buffers;
  * synchronises the device.  Not for use under stream capture. */
 int mhdgpu_autotune(int nx, int ny, int nz, int math);
+
+/* ------------------------------------------------------------------------
+ * FP64 diagnostics of a state (the reference prints float sums from the host,
+ * Heterogeneous_MHD/C/check_value.c:22-79).  d_out (device, 8 doubles):
+ *   [0..4] sums of rho, m_x, m_y, m_z, E over the box;
+ *   [5]    max |div B| = |b1(i+1)-b1(i) + b2(j+1)-b2(j) + b3(k+1)-b3(k)|;
+ *   [6]    min gas pressure p = (gamma-1)(E - m^2/2rho - Bc^2/2), Bc the
+ *          face field averaged to the cell centre as fluidx does;
+ *   [7]    number of cells with p <= 0.
+ * Every term and partial sum is a double; the order is fixed by the box size,
+ * so results repeat bit for bit.  d_scratch holds
+ * mhdgpu_diagnostics_scratch_bytes(nx, ny, nz) bytes (<= 40 KB).
+ * ------------------------------------------------------------------------ */
+#define MHD_DIAG_COUNT 8
+size_t mhdgpu_diagnostics_scratch_bytes(int nx, int ny, int nz);
+int mhdgpu_diagnostics(const float *u, const float *b, int nx, int ny, int nz, double *d_out,
+                       void *d_scratch, mhdgpu_stream_t stream);
+
+/* ------------------------------------------------------------------------
+ * State files in the reference's formats (host arrays in the reference
+ * layout; the reference hard-codes sizes and file names, these take both):
+ *   mhdgpu_read_state / mhdgpu_write_state: the init file of
+ *     Heterogeneous_MHD/C/init.c:33-66 -- raw float32, cells x-outer,
+ *     z-inner, 8 floats each (rho, m_x, m_y, m_z, E, b_x, b_y, b_z); a run
+ *     checkpoints with write_state and resumes with read_state;
+ *   mhdgpu_write_result: the final dump of C/mhd.c:126-160 -- two raw files,
+ *     u (5 floats per cell) and b (3), cells x-outer, z-inner;
+ *   mhdgpu_write_check: the check dump of C/check_value.c:22-79 -- eight text
+ *     files <prefix>u1.dat .. <prefix>b3.dat, "%8.6e" per line, x fastest.
+ * MHD_ERR_ARG on bad arguments or a file of the wrong size, MHD_ERR_NOMEM on
+ * an I/O failure.
+ * ------------------------------------------------------------------------ */
+int mhdgpu_read_state(const char *path, float *u, float *b, int nx, int ny, int nz);
+int mhdgpu_write_state(const char *path, const float *u, const float *b, int nx, int ny, int nz);
+int mhdgpu_write_result(const char *path_u, const char *path_b, const float *u, const float *b,
+                        int nx, int ny, int nz);
+int mhdgpu_write_check(const char *prefix, const float *u, const float *b, int nx, int ny, int nz);
 
 /* ------------------------------------------------------------------------
  * Batched ensemble (no counterpart in the reference, whose drivers advance

@@ -2,7 +2,7 @@
 
     python mhd-gpu_gb300/build.py [--verbose-ptxas]
 
-Each .cu in csrc/ is compiled in parallel to an object under _build/ and the
+Each .cu (and host-only .cpp) in csrc/ is compiled in parallel to an object under _build/ and the
 objects are linked into lib/libmhdgpu.so.  A file is rebuilt when it or any
 header is newer than its object.
 """
@@ -45,15 +45,22 @@ def _stale(src: str, obj: str, deps) -> bool:
     return any(os.path.getmtime(d) > t for d in [src, *deps])
 
 
+def _obj(src: str) -> str:
+    return os.path.join(BUILD, os.path.splitext(os.path.basename(src))[0] + ".o")
+
+
 def build(verbose_ptxas: bool = False, quiet: bool = True) -> str:
     os.makedirs(BUILD, exist_ok=True)
     os.makedirs(LIBDIR, exist_ok=True)
-    srcs = sorted(glob.glob(os.path.join(CSRC, "*.cu")))
+    srcs = sorted(glob.glob(os.path.join(CSRC, "*.cu")) + glob.glob(os.path.join(CSRC, "*.cpp")))
+    # the heaviest translation units first, so the parallel build ends sooner
+    heavy = ("batch_", "fluidx", "advect")
+    srcs.sort(key=lambda s: (not os.path.basename(s).startswith(heavy), s))
     deps = _headers()
     cc = nvcc()
     jobs = []
     for s in srcs:
-        o = os.path.join(BUILD, os.path.basename(s)[:-3] + ".o")
+        o = _obj(s)
         if verbose_ptxas or _stale(s, o, deps):
             cmd = [cc, *NVFLAGS, "-c", s, "-o", o]
             if verbose_ptxas:
@@ -66,7 +73,7 @@ def build(verbose_ptxas: bool = False, quiet: bool = True) -> str:
         return s, r
 
     failed = []
-    with cf.ThreadPoolExecutor(max_workers=min(8, max(1, len(jobs)))) as ex:
+    with cf.ThreadPoolExecutor(max_workers=min(os.cpu_count() or 8, 16, max(1, len(jobs)))) as ex:
         for s, r in ex.map(run, jobs):
             if r.returncode != 0:
                 failed.append((s, r.stderr))
@@ -75,7 +82,7 @@ def build(verbose_ptxas: bool = False, quiet: bool = True) -> str:
     if failed:
         msg = "\n".join(f"--- {s}\n{e}" for s, e in failed)
         raise RuntimeError("nvcc failed:\n" + msg)
-    objs = [os.path.join(BUILD, os.path.basename(s)[:-3] + ".o") for s in srcs]
+    objs = [_obj(s) for s in srcs]
     if jobs or not os.path.exists(LIB) or any(os.path.getmtime(o) > os.path.getmtime(LIB) for o in objs):
         cmd = [cc, *ARCH, "-shared", "-o", LIB, *objs, "-lcudart", "-Xlinker", "-Bsymbolic"]
         r = subprocess.run(cmd, capture_output=True, text=True)

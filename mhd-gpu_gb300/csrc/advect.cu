@@ -63,7 +63,7 @@ static cudaError_t launch_advect_shape(const AdvectArgs &a, int ppc, bool rows, 
 template <class M>
 static cudaError_t launch_advect_policy(const AdvectArgs &a, const PencilCfg &cfg, cudaStream_t s)
 {
-    const bool rows = a.f.si != 1;
+    const bool rows = frame_rows(a.f);
 #define MHD_AX(C, W) \
     if (cfg.cpl == C && cfg.wpp == W) return launch_advect_shape<C, W, M>(a, cfg.ppc, rows, s);
     MHD_PENCIL_SHAPES(MHD_AX)

@@ -84,18 +84,19 @@ struct mhdgpu_batch {
     int nctr = 0;
     unsigned *d_abort = nullptr;
     long long *d_start = nullptr;       // 6 x (3*nbox + 1)
+    int *d_group = nullptr;             // 6 x 3*nbox
     long long *d_cfl_start = nullptr;   // nbox + 1
     long long cfl_total = 0;
     long long total[6] = {};
     int threads[3] = {256, 256, 256};
-    int cps[3] = {2, 2, 2};             // requested CTAs per SM
+    int cps[3] = {3, 3, 3};             // requested CTAs per SM
     int grid[6] = {};
     size_t smem[3] = {};
 
     ~mhdgpu_batch()
     {
         cudaFree(d_box); cudaFree(d_clk); cudaFree(d_scr); cudaFree(d_tf);
-        cudaFree(d_ctr); cudaFree(d_start); cudaFree(d_cfl_start);
+        cudaFree(d_ctr); cudaFree(d_start); cudaFree(d_group); cudaFree(d_cfl_start);
     }
 };
 
@@ -134,8 +135,11 @@ long long cells_of(const int *d) { return (long long)d[0] * d[1] * d[2]; }
 
 int occupancy(bool rows, int threads, size_t smem)
 {
-    return math_mode() == MHD_MATH_FAST ? batch_sweep_occupancy_fast(rows, threads, smem)
-                                        : batch_sweep_occupancy_faithful(rows, threads, smem);
+    switch (math_mode()) {
+    case MHD_MATH_FAST: return batch_sweep_occupancy_fast(rows, threads, smem);
+    case MHD_MATH_FP64P: return batch_sweep_occupancy_p64(rows, threads, smem);
+    default: return batch_sweep_occupancy_faithful(rows, threads, smem);
+    }
 }
 
 // dynamic shared memory of a sweep along axis with `threads` per CTA: the
@@ -159,6 +163,7 @@ int build_tables(mhdgpu_batch &bt)
 {
     const int nb = bt.nbox;
     std::vector<long long> start(6 * (size_t)(3 * nb + 1));
+    std::vector<int> group(6 * (size_t)(3 * nb));
     for (int s = 0; s < 6; ++s) {
         const int axis = kSweepAxis[s];
         const bool rows = axis != 0;
@@ -175,7 +180,18 @@ int build_tables(mhdgpu_batch &bt)
                     return bfail(MHD_ERR_ARG, "mhdgpu_batch: fewer threads per CTA than a pencil's team "
                                               "(64 for pencils of 65-127 cells, 128 above 128)");
                 st[slot * nb + i] = acc;
-                acc += ph == kPhaseB1 ? batch_chunks(f.npen * f.n, threads * 8) : batch_tiles(f, ppc, rows);
+                int g;
+                long long items;
+                if (ph == kPhaseB1) {
+                    g = kB1ItemCells;
+                    items = batch_chunks(f.npen * f.n, g);
+                } else {
+                    const long long tiles = batch_tiles(f, ppc, rows);
+                    g = std::max(1, kItemCells / (ppc * f.n));
+                    items = (tiles + g - 1) / g;
+                }
+                group[(size_t)s * 3 * nb + slot * nb + i] = g;
+                acc += items;
             }
         }
         st[3 * nb] = acc;
@@ -193,6 +209,8 @@ int build_tables(mhdgpu_batch &bt)
                 bt.grid[s] = (int)std::max(1LL, std::min((long long)bt.num_sms * cps, bt.total[s]));
     }
     BCU(cudaMemcpy(bt.d_start, start.data(), start.size() * sizeof(long long), cudaMemcpyHostToDevice),
+        "mhdgpu_batch tables");
+    BCU(cudaMemcpy(bt.d_group, group.data(), group.size() * sizeof(int), cudaMemcpyHostToDevice),
         "mhdgpu_batch tables");
     return MHD_OK;
 }
@@ -216,19 +234,20 @@ int launch_step(mhdgpu_batch &bt, cudaStream_t s, cudaEvent_t *ev /* 7 events or
         SweepWork w;
         w.box = bt.d_box;
         w.start = bt.d_start + (size_t)sw * (3 * nb + 1);
+        w.group = bt.d_group + (size_t)sw * 3 * nb;
         w.claim = bt.d_ctr + sw;
         w.done = bt.d_ctr + 6 + (size_t)sw * 3 * nb;
         w.abort = bt.d_abort;
         w.nbox = nb;
         w.axis = axis;
         w.fluid_first = kSweepFluidFirst[sw];
-        w.b1_chunk = bt.threads[axis] * 8;
         if (ev) BCU(cudaEventRecord(ev[sw], s), "mhdgpu_batch event");
         ProfScope ps(MHD_KCLASS_BATCH, 1, s);
+        const bool rows = axis != 0;
         const cudaError_t e =
-            math == MHD_MATH_FAST
-                ? launch_batch_sweep_fast(w, axis != 0, bt.grid[sw], bt.threads[axis], bt.smem[axis], s)
-                : launch_batch_sweep_faithful(w, axis != 0, bt.grid[sw], bt.threads[axis], bt.smem[axis], s);
+            math == MHD_MATH_FAST    ? launch_batch_sweep_fast(w, rows, bt.grid[sw], bt.threads[axis], bt.smem[axis], s)
+            : math == MHD_MATH_FP64P ? launch_batch_sweep_p64(w, rows, bt.grid[sw], bt.threads[axis], bt.smem[axis], s)
+                                     : launch_batch_sweep_faithful(w, rows, bt.grid[sw], bt.threads[axis], bt.smem[axis], s);
         BCU(e, "mhdgpu_batch_advance sweep");
     }
     if (ev) BCU(cudaEventRecord(ev[6], s), "mhdgpu_batch event");
@@ -246,7 +265,8 @@ size_t mhdgpu_batch_workspace_bytes(int nbox, const int *dims)
     for (int i = 0; i < nbox; ++i) cells += cells_of(dims + 3 * i);
     const size_t nctr = 6 + 18 * (size_t)nbox + 1;
     return sizeof(float) * 2 * (size_t)cells + nbox * (sizeof(BoxDesc) + sizeof(mhdgpu_clock) + sizeof(float)) +
-           nctr * sizeof(unsigned) + (6 * (3 * (size_t)nbox + 1) + nbox + 1) * sizeof(long long);
+           nctr * sizeof(unsigned) + (6 * (3 * (size_t)nbox + 1) + nbox + 1) * sizeof(long long) +
+           18 * (size_t)nbox * sizeof(int);
 }
 
 int mhdgpu_batch_create(mhdgpu_batch **out, int nbox, const int *dims, float *const *d_u,
@@ -286,6 +306,7 @@ int mhdgpu_batch_create(mhdgpu_batch **out, int nbox, const int *dims, float *co
     if (e == cudaSuccess) e = cudaMalloc(&bt->d_tf, nbox * sizeof(float));
     if (e == cudaSuccess) e = cudaMalloc(&bt->d_ctr, (bt->nctr + 1) * sizeof(unsigned));
     if (e == cudaSuccess) e = cudaMalloc(&bt->d_start, 6 * (3 * (size_t)nbox + 1) * sizeof(long long));
+    if (e == cudaSuccess) e = cudaMalloc(&bt->d_group, 6 * 3 * (size_t)nbox * sizeof(int));
     if (e == cudaSuccess) e = cudaMalloc(&bt->d_cfl_start, (nbox + 1) * sizeof(long long));
     if (e != cudaSuccess) {
         delete bt;

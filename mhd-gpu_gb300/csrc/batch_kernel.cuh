@@ -21,11 +21,13 @@
 //
 // Team classes.  One kernel serves every pencil length of a sweep: the team
 // shape is picked per item from the box's pencil length, with the length a
-// compile-time constant where one warp fills it (32, 64, 96, 128 cells), and
-// at most two cells per thread otherwise.  Each class's tile is a separate
-// (not inlined) function: inlined together in one kernel the classes spill
-// registers that each of them alone does not need, and the call costs once per
-// tile.  The kernel's item arguments are staged in shared memory.
+// compile-time constant for the ensemble's sizes (32, 48, 64, 96, 128) and at
+// most three cells per thread.  Each class's tile is a separate (not inlined)
+// function: inlined together in one kernel the classes spill registers that
+// each of them alone does not need, and the call costs once per tile.  The
+// kernel runs at 80 registers (3 CTAs of 256 threads per SM), where the
+// full-team classes do not spill.  The item arguments are staged in shared
+// memory.
 #pragma once
 
 #include "advect_kernel.cuh"
@@ -43,26 +45,27 @@ struct BoxDesc {
     int nx, ny, nz, pad;
 };
 
-// team class by pencil length (1 <= n <= kBatchMaxPencil):
-//   0-3: n = 32, 64, 96, 128, one warp with 1-4 cells per thread, n fixed;
-//   4: n < 32 (1 cell, one warp); 5: n < 64 (2 cells, one warp);
-//   6: other n < 128 (2 cells, two warps); 7: n <= 256 (2 cells, four warps)
+// team class by pencil length (1 <= n <= kBatchMaxPencil); the length is a
+// compile-time constant for 32, 48, 64, 96 and 128 cells:
+//   0: 32 = 1 x 32 threads     1: 64 = 2 x 32      2: 96 = 3 x 32
+//   3: 128 = 2 x 64            4: 48 (2 x 32, 16 slots idle)
+//   5: other n < 64 (2 x 32)   6: other n < 128 (2 x 64)   7: n <= 256 (2 x 128)
 __host__ __device__ inline int batch_class(int n)
 {
-    if (n == 32) return 0;
-    if (n == 64) return 1;
-    if (n == 96) return 2;
-    if (n == 128) return 3;
-    if (n < 32) return 4;
-    if (n < 64) return 5;
-    if (n < 128) return 6;
-    return 7;
+    switch (n) {
+    case 32: return 0;
+    case 64: return 1;
+    case 96: return 2;
+    case 128: return 3;
+    case 48: return 4;
+    default: return n < 64 ? 5 : (n < 128 ? 6 : 7);
+    }
 }
 // threads per pencil of the class
 __host__ __device__ inline int batch_tpp(int n)
 {
     const int c = batch_class(n);
-    return c == 6 ? 64 : (c == 7 ? 128 : 32);
+    return (c == 3 || c == 6) ? 64 : (c == 7 ? 128 : 32);
 }
 
 // items of a phase: tiles of ppc pencils (contiguous pencils are numbered
@@ -85,17 +88,30 @@ __host__ __device__ inline int batch_phase(int slot, int fluid_first)
 struct SweepWork {
     const BoxDesc *box;
     const long long *start;   // 3*nbox + 1 prefix sums of item counts, entry slot*nbox + box
+    const int *group;         // 3*nbox: tiles per item (fluid, field) or cells per item (b(1))
     unsigned *claim;          // next item of this launch (zeroed by the clock kernel)
     unsigned *done;           // 3*nbox items finished per (slot, box) (zeroed likewise)
     unsigned *abort;          // nonzero once a dependency wait gave up
-    int nbox, axis, fluid_first, b1_chunk;
+    int nbox, axis, fluid_first;
 };
+
+// an item covers about this many cells (several tiles of small pencils), so
+// the claim and the completion count cost little against the item's work
+constexpr int kItemCells = 2048;
+constexpr int kB1ItemCells = 4096;
 
 __device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned *p)
 {
     unsigned v;
     asm volatile("ld.acquire.gpu.global.u32 %0, [%1];\n" : "=r"(v) : "l"(p) : "memory");
     return v;
+}
+
+// count an item done: a release reduction (no round trip), ordered after the
+// CTA's writes by the barrier that precedes it
+__device__ __forceinline__ void red_release_add(unsigned *p, unsigned v)
+{
+    asm volatile("red.release.gpu.global.add.u32 [%0], %1;\n" ::"l"(p), "r"(v) : "memory");
 }
 
 __device__ __forceinline__ unsigned long long global_ns()
@@ -144,8 +160,8 @@ __device__ __forceinline__ void batch_fluidx(const FluidxArgs &a, long long tile
     case 0: batch_fluidx_class<1, 1, M, ROWS, 32>(a, tile); break;
     case 1: batch_fluidx_class<2, 1, M, ROWS, 64>(a, tile); break;
     case 2: batch_fluidx_class<3, 1, M, ROWS, 96>(a, tile); break;
-    case 3: batch_fluidx_class<4, 1, M, ROWS, 128>(a, tile); break;
-    case 4: batch_fluidx_class<1, 1, M, ROWS, 0>(a, tile); break;
+    case 3: batch_fluidx_class<2, 2, M, ROWS, 128>(a, tile); break;
+    case 4: batch_fluidx_class<2, 1, M, ROWS, 48>(a, tile); break;
     case 5: batch_fluidx_class<2, 1, M, ROWS, 0>(a, tile); break;
     case 6: batch_fluidx_class<2, 2, M, ROWS, 0>(a, tile); break;
     default: batch_fluidx_class<2, 4, M, ROWS, 0>(a, tile); break;
@@ -159,27 +175,25 @@ __device__ __forceinline__ void batch_advect(const AdvectArgs &a, long long tile
     case 0: batch_advect_class<1, 1, M, ROWS, 32>(a, tile); break;
     case 1: batch_advect_class<2, 1, M, ROWS, 64>(a, tile); break;
     case 2: batch_advect_class<3, 1, M, ROWS, 96>(a, tile); break;
-    case 3: batch_advect_class<4, 1, M, ROWS, 128>(a, tile); break;
-    case 4: batch_advect_class<1, 1, M, ROWS, 0>(a, tile); break;
+    case 3: batch_advect_class<2, 2, M, ROWS, 128>(a, tile); break;
+    case 4: batch_advect_class<2, 1, M, ROWS, 48>(a, tile); break;
     case 5: batch_advect_class<2, 1, M, ROWS, 0>(a, tile); break;
     case 6: batch_advect_class<2, 2, M, ROWS, 0>(a, tile); break;
     default: batch_advect_class<2, 4, M, ROWS, 0>(a, tile); break;
     }
 }
 
-__device__ __forceinline__ void batch_b1(const AdvectArgs &a, long long chunk, int chunk_cells)
+__device__ __forceinline__ void batch_b1(const AdvectArgs &a, long long c0, int cells)
 {
     const long long ncell = a.f.npen * a.f.n;
-    const long long c0 = chunk * chunk_cells;
-    const long long c1 = min(c0 + chunk_cells, ncell);
+    const long long c1 = min(c0 + cells, ncell);
     for (long long c = c0 + threadIdx.x; c < c1; c += blockDim.x) advect_b1_cell(a.b, a.sA, a.sB, a.f, c);
 }
 
 // One sweep of every box.  At most 256 threads (8 pencils of one warp per
-// CTA); 2 CTAs per SM bound the registers at 128, which the full-team classes
-// use without spilling.
+// CTA); 3 CTAs per SM bound the registers at 80.
 template <class M, bool ROWS>
-__global__ void __launch_bounds__(256, 2)
+__global__ void __launch_bounds__(256, 3)
 batch_sweep_kernel(SweepWork w)
 {
     __shared__ int s_e, s_run;
@@ -187,36 +201,37 @@ batch_sweep_kernel(SweepWork w)
     __shared__ FluidxArgs s_fa;
     __shared__ AdvectArgs s_aa;
     const long long total = w.start[3 * w.nbox];
+    // thread 0 claims the next item while the CTA works on the current one
+    unsigned it = 0;
+    if (threadIdx.x == 0) it = atomicAdd(w.claim, 1u);
     for (;;) {
         if (threadIdx.x == 0) {
-            const long long it = (long long)atomicAdd(w.claim, 1u);
             int e = -1, run = 0;
             long long local = 0;
-            if (it < total) {
+            if ((long long)it < total) {
                 int lo = 0, hi = 3 * w.nbox - 1;   // last entry with start <= it
                 while (lo < hi) {
                     const int mid = (lo + hi + 1) >> 1;
-                    if (w.start[mid] <= it) lo = mid;
+                    if (w.start[mid] <= (long long)it) lo = mid;
                     else hi = mid - 1;
                 }
                 e = lo;
-                local = it - w.start[e];
+                local = (long long)it - w.start[e];
                 run = 1;
                 if (e >= w.nbox) {   // wait for the box's previous phase
                     const int prev = e - w.nbox;
                     const unsigned need = (unsigned)(w.start[prev + 1] - w.start[prev]);
                     run = batch_wait(w.done + prev, need, w.abort, &w.box[e % w.nbox].clk->health);
                 }
-            }
-            s_e = e;
-            s_run = run;
-            s_local = local;
-            if (e >= 0) {
                 const BoxDesc d = w.box[e % w.nbox];
                 const Frame f = make_view(w.axis, d.nx, d.ny, d.nz);
                 s_fa = FluidxArgs{d.u, d.u, d.b, &d.clk->dt, &d.clk->health, f};
                 s_aa = AdvectArgs{d.b, d.u, &d.clk->dt, d.scr, d.scr + f.npen * f.n, f};
+                it = atomicAdd(w.claim, 1u);
             }
+            s_e = e;
+            s_run = run;
+            s_local = local;
         }
         __syncthreads();
         const int e = s_e;
@@ -224,16 +239,23 @@ batch_sweep_kernel(SweepWork w)
         if (s_run) {
             const int ph = batch_phase(e / w.nbox, w.fluid_first);
             const long long local = s_local;
-            if (ph == kPhaseFluid) batch_fluidx<M, ROWS>(s_fa, local);
-            else if (ph == kPhaseField) batch_advect<M, ROWS>(s_aa, local);
-            else batch_b1(s_aa, local, w.b1_chunk);
+            const int g = w.group[e];
+            if (ph == kPhaseB1) {
+                batch_b1(s_aa, local * g, g);
+            } else {
+                const int ppc = blockDim.x / batch_tpp(s_fa.f.n);
+                const long long t0 = local * g;
+                const long long t1 = min(t0 + g, batch_tiles(s_fa.f, ppc, ROWS));
+                for (long long t = t0; t < t1; ++t) {
+                    if (t > t0) __syncthreads();   // the previous tile's shared memory is consumed
+                    if (ph == kPhaseFluid) batch_fluidx<M, ROWS>(s_fa, t);
+                    else batch_advect<M, ROWS>(s_aa, t);
+                }
+            }
         }
-        // every write of the item is issued; publish them, then count the item
+        // every write of the item is issued; count it with release semantics
         __syncthreads();
-        if (threadIdx.x == 0) {
-            __threadfence();
-            atomicAdd(w.done + e, 1u);
-        }
+        if (threadIdx.x == 0) red_release_add(w.done + e, 1u);
     }
 }
 
@@ -266,12 +288,15 @@ int batch_sweep_occupancy_inst(int threads, size_t smem)
     return nb;
 }
 
-// per-policy launchers (batch_faithful.cu, batch_fast.cu)
+// per-policy launchers (batch_faithful.cu, batch_fast.cu, batch_p64.cu)
 cudaError_t launch_batch_sweep_faithful(const SweepWork &w, bool rows, int grid, int threads, size_t smem,
                                         cudaStream_t s);
 cudaError_t launch_batch_sweep_fast(const SweepWork &w, bool rows, int grid, int threads, size_t smem,
                                     cudaStream_t s);
 int batch_sweep_occupancy_faithful(bool rows, int threads, size_t smem);
 int batch_sweep_occupancy_fast(bool rows, int threads, size_t smem);
+cudaError_t launch_batch_sweep_p64(const SweepWork &w, bool rows, int grid, int threads, size_t smem,
+                                   cudaStream_t s);
+int batch_sweep_occupancy_p64(bool rows, int threads, size_t smem);
 
 }  // namespace mhd

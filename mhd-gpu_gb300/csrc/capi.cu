@@ -238,11 +238,11 @@ static int sweep_view(float *u, float *b, const Frame &f, const float *dt, float
     for (int part = 0; part < 2; ++part) {
         if ((part == 0) == fluid_first) {
             ProfScope ps(MHD_KCLASS_FLUIDX, 1, s);
-            MHD_CU(launch_fluidx(fa, pencil_cfg(MHD_KCLASS_FLUIDX, f.n, f.si != 1), math_mode(), s),
+            MHD_CU(launch_fluidx(fa, pencil_cfg(MHD_KCLASS_FLUIDX, f.n, frame_rows(f)), math_mode(), s),
                    "fused fluidx");
         } else {
             ProfScope ps(MHD_KCLASS_ADVECT, 2, s);
-            MHD_CU(launch_advect(aa, pencil_cfg(MHD_KCLASS_ADVECT, f.n, f.si != 1), math_mode(), s),
+            MHD_CU(launch_advect(aa, pencil_cfg(MHD_KCLASS_ADVECT, f.n, frame_rows(f)), math_mode(), s),
                    "fused advectbyzx");
         }
     }

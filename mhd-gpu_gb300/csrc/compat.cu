@@ -17,6 +17,7 @@
 
 #include "mhdgpu.h"
 #include "mhdgpu_compat.h"
+#include "mhdgpu_fortran.h"
 
 namespace {
 
@@ -153,6 +154,61 @@ void copy_matrix(float *u, float *b, int *nx, int *ny, int *nz, float *update_u,
     const size_t nc = cells(nx, ny, nz);
     memcpy(update_u, u, nc * 5 * sizeof(float));
     memcpy(update_b, b, nc * 3 * sizeof(float));
+}
+
+// ---- Fortran ABI (include/mhdgpu_fortran.h): the external subroutines of
+// OpenMP/mhd.f90:249-474 as gfortran names them (lower case, trailing
+// underscore, every argument by reference), host arrays, synchronous.
+
+void fluidx_(float *u, float *b, int *nx, int *ny, int *nz, float *dt)
+{
+    const size_t nc = cells(nx, ny, nz);
+    if (!g_ctx.ensure(nc)) { report(MHD_ERR_NOMEM, "fluidx_"); return; }
+    if (!cuda_ok(cudaMemcpy(g_ctx.du, u, nc * 5 * sizeof(float), cudaMemcpyHostToDevice), "fluidx_")) return;
+    if (!cuda_ok(cudaMemcpy(g_ctx.db, b, nc * 3 * sizeof(float), cudaMemcpyHostToDevice), "fluidx_")) return;
+    if (!cuda_ok(cudaMemcpy(g_ctx.dt, dt, sizeof(float), cudaMemcpyHostToDevice), "fluidx_")) return;
+    if (!report(mhdgpu_fluidx(g_ctx.du, g_ctx.du, g_ctx.db, *nx, *ny, *nz, g_ctx.dt, nullptr, nullptr), "fluidx_")) return;
+    cuda_ok(cudaMemcpy(u, g_ctx.du, nc * 5 * sizeof(float), cudaMemcpyDeviceToHost), "fluidx_");
+}
+
+void advectbyzx_(float *u, float *b, int *nx, int *ny, int *nz, float *dt)
+{
+    const size_t nc = cells(nx, ny, nz);
+    if (!g_ctx.ensure(nc)) { report(MHD_ERR_NOMEM, "advectbyzx_"); return; }
+    if (!cuda_ok(cudaMemcpy(g_ctx.du, u, nc * 5 * sizeof(float), cudaMemcpyHostToDevice), "advectbyzx_")) return;
+    if (!cuda_ok(cudaMemcpy(g_ctx.db, b, nc * 3 * sizeof(float), cudaMemcpyHostToDevice), "advectbyzx_")) return;
+    if (!cuda_ok(cudaMemcpy(g_ctx.dt, dt, sizeof(float), cudaMemcpyHostToDevice), "advectbyzx_")) return;
+    if (!report(mhdgpu_advectbyzx(g_ctx.db, g_ctx.du, *nx, *ny, *nz, g_ctx.dt, g_ctx.scr, nullptr), "advectbyzx_"))
+        return;
+    cuda_ok(cudaMemcpy(b, g_ctx.db, nc * 3 * sizeof(float), cudaMemcpyDeviceToHost), "advectbyzx_");
+}
+
+// The Fortran driver transposes in place, transpose12(u,b,u,b,...): the
+// shim reads the whole input before it writes the output, so ut may be u.
+void transpose12_(float *ut, float *bt, float *u, float *b, int *nx, int *ny, int *nz)
+{
+    transpose_shim(ut, bt, u, b, nx, ny, nz, 12, "transpose12_");
+}
+
+void transpose13_(float *ut, float *bt, float *u, float *b, int *nx, int *ny, int *nz)
+{
+    transpose_shim(ut, bt, u, b, nx, ny, nz, 13, "transpose13_");
+}
+
+// The Fortran cfl (mhd.f90:96-125) is internal to the main program and sees
+// the sizes by host association; as an external function it takes them.
+// Release 0.2 formula (B averaged to the cell centre); returns 1/c.
+float cfl_(float *u, float *b, int *nx, int *ny, int *nz)
+{
+    const size_t nc = cells(nx, ny, nz);
+    float inv = 0.0f;
+    if (!g_ctx.ensure(nc)) { report(MHD_ERR_NOMEM, "cfl_"); return inv; }
+    if (!cuda_ok(cudaMemcpy(g_ctx.du, u, nc * 5 * sizeof(float), cudaMemcpyHostToDevice), "cfl_")) return inv;
+    if (!cuda_ok(cudaMemcpy(g_ctx.db, b, nc * 3 * sizeof(float), cudaMemcpyHostToDevice), "cfl_")) return inv;
+    if (!report(mhdgpu_cfl(g_ctx.du, g_ctx.db, *nx, *ny, *nz, MHD_CFL_AVERAGED, g_ctx.dt, g_ctx.word, nullptr), "cfl_"))
+        return inv;
+    cuda_ok(cudaMemcpy(&inv, g_ctx.dt, sizeof(float), cudaMemcpyDeviceToHost), "cfl_");
+    return inv;
 }
 
 }  // extern "C"

@@ -25,7 +25,7 @@ cudaError_t launch_fluidx_faithful(const FluidxArgs &a, const PencilCfg &cfg, cu
 // with identity component maps, or pencils across memory with sj == 1
 bool frame_supported(const Frame &f)
 {
-    if (f.si == 1)
+    if (!frame_rows(f))
         return f.sj == f.n && f.sk == (long long)f.n * f.ny && f.pu == 0x43210u && f.pb == 0x210u;
     return f.sj == 1;
 }
@@ -34,6 +34,7 @@ cudaError_t launch_fluidx(const FluidxArgs &a, const PencilCfg &cfg, int math, c
 {
     if (!pencil_shape_ok(cfg, a.f.n) || !frame_supported(a.f)) return cudaErrorInvalidConfiguration;
     if (math == MHD_MATH_FAST) return launch_fluidx_fast(a, cfg, s);
+    if (math == MHD_MATH_FP64P) return launch_fluidx_p64(a, cfg, s);
     return launch_fluidx_faithful(a, cfg, s);
 }
 

@@ -370,7 +370,7 @@ cudaError_t launch_fluidx_inst(const FluidxArgs &a, int ppc, cudaStream_t s)
 }
 
 // dispatch over the supported team shapes, both staging modes (rows mode
-// when the frame's pencils run across memory, sj == 1 and si != 1) and the
+// when the frame's pencils run across memory, frame_rows) and the
 // compile-time length when the pencil fills the team exactly
 template <int C, int W, class M>
 cudaError_t launch_fluidx_shape(const FluidxArgs &a, int ppc, bool rows, cudaStream_t s)
@@ -386,7 +386,7 @@ cudaError_t launch_fluidx_shape(const FluidxArgs &a, int ppc, bool rows, cudaStr
 template <class M>
 cudaError_t launch_fluidx_policy(const FluidxArgs &a, const PencilCfg &cfg, cudaStream_t s)
 {
-    const bool rows = a.f.si != 1;
+    const bool rows = frame_rows(a.f);
 #define MHD_FX(C, W) \
     if (cfg.cpl == C && cfg.wpp == W) return launch_fluidx_shape<C, W, M>(a, cfg.ppc, rows, s);
     MHD_PENCIL_SHAPES(MHD_FX)

@@ -55,6 +55,7 @@ int math_mode();
 cudaError_t launch_fluidx(const FluidxArgs &a, const PencilCfg &cfg, int math, cudaStream_t s);
 cudaError_t launch_fluidx_faithful(const FluidxArgs &a, const PencilCfg &cfg, cudaStream_t s);
 cudaError_t launch_fluidx_fast(const FluidxArgs &a, const PencilCfg &cfg, cudaStream_t s);
+cudaError_t launch_fluidx_p64(const FluidxArgs &a, const PencilCfg &cfg, cudaStream_t s);
 cudaError_t launch_advect(const AdvectArgs &a, const PencilCfg &cfg, int math, cudaStream_t s);
 cudaError_t launch_transpose(float *du, float *db, const float *su, const float *sb,
                              int nx, int ny, int nz, int which, cudaStream_t s);

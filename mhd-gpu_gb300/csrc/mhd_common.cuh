@@ -61,6 +61,15 @@ __host__ __device__ inline Frame make_view(int axis, int nx, int ny, int nz)
 
 __host__ __device__ __forceinline__ int nib(unsigned m, int f) { return (int)((m >> (4 * f)) & 15u); }
 
+// Staging mode of a frame: contiguous pencils (the reference layout seen as
+// itself: si = 1 and identity component maps) or rows (any other view; its
+// pencils run across memory with sj = 1).  A y or z view of a box with
+// nx = 1 has si = 1 too, but permuted components: it is staged in rows.
+__host__ __device__ inline bool frame_rows(const Frame &f)
+{
+    return !(f.si == 1 && f.pu == 0x43210u && f.pb == 0x210u);
+}
+
 // A team of TPP = 32*WPP threads owns one pencil; thread t holds the CPL
 // cells c = m*TPP + t (m < CPL).  Cells >= n are padding: they compute on
 // harmless values and are never reduced or stored.  NT > 0 is the pencil

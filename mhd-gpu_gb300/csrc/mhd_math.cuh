@@ -153,6 +153,15 @@ struct Faithful {
         return ffma(e, y, q0);
     }
     MHD_HD static float pressure(float e, float q, float b2) { return total_pressure(e, q, b2); }
+    // total pressure ps (mhdflux.c:26-29) and gas pressure p = ps - B^2/2
+    // (mhdflux.c:39-42) of a cell; s2 = |m|^2, b2 = |B|^2, yr = RN(1/rho)
+    MHD_HD static void recover(const float u[5], const float bc[3], float yr, float s2, float b2,
+                               float &ps, float &p)
+    {
+        (void)bc;
+        ps = pressure(u[4], divy(s2, u[0], yr), b2);
+        p = fsub(ps, 0.5f * b2);
+    }
     // RN(x + sqrt(a)) with the root in float-float: zh ~ sqrt(a) from the
     // hardware rsqrt, zl = (a - zh^2)/(2 zh) with the exact FMA residual.
     MHD_HD static float speed(float x, float a)
@@ -188,7 +197,38 @@ struct Fast {
     {
         return (e - 0.5f * q) * kGammaM1 + b2 * kTwoMGammaHalf;
     }
+    MHD_HD static void recover(const float u[5], const float bc[3], float yr, float s2, float b2,
+                               float &ps, float &p)
+    {
+        (void)bc;
+        ps = pressure(u[4], divy(s2, u[0], yr), b2);
+        p = ps - 0.5f * b2;
+    }
     MHD_HD static float speed(float x, float a) { return (a > 0.0f) ? x + a * rsqrt_approx(a) : x; }
+};
+
+// Faithful arithmetic except for the pressure of low-beta cells, which is
+// recovered in FP64: where the FP32 gas pressure gives beta = 2p/B^2 below
+// kLowBeta (or p <= 0), p = (gamma-1)(E - |m|^2/(2 rho) - |B|^2/2) is formed
+// in double from the cell's float state and ps = p + |B|^2/2, both rounded
+// once to float.  At low beta the FP32 chain ps -> p = ps - B^2/2 cancels
+// (ps ~ B^2/2 >> p); the double chain does not.  gamma is the solver's float
+// constant.  Costs ~15 FP64 operations (one divide) per low-beta cell-flux.
+constexpr float kLowBeta = 0.1f;
+struct Recover64 : Faithful {
+    MHD_HD static void recover(const float u[5], const float bc[3], float yr, float s2, float b2,
+                               float &ps, float &p)
+    {
+        Faithful::recover(u, bc, yr, s2, b2, ps, p);
+        if (p >= kLowBeta * 0.5f * b2) return;
+        const double bx = bc[0], by = bc[1], bz = bc[2];
+        const double m1 = u[1], m2 = u[2], m3 = u[3];
+        const double b2d = bx * bx + by * by + bz * bz;
+        const double qd = (m1 * m1 + m2 * m2 + m3 * m3) / (double)u[0];
+        const double pd = ((double)kGamma - 1.0) * ((double)u[4] - 0.5 * qd - 0.5 * b2d);
+        p = (float)pd;
+        ps = (float)(pd + 0.5 * b2d);
+    }
 };
 
 // Fluxes v (not yet divided by the pencil's c) and fast speed of one cell
@@ -203,14 +243,15 @@ MHD_HD void cell_flux(const float u[5], const float bc[3], float v[5], float &cs
     const float vx = M::divy(m1, r, yr);
     const float b2 = M::add(M::add(M::mul(bx, bx), M::mul(by, by)), M::mul(bz, bz));
     const float s2 = M::add(M::add(M::mul(m1, m1), M::mul(m2, m2)), M::mul(m3, m3));
-    const float ps = M::pressure(e, M::divy(s2, r, yr), b2);
+    float ps, pg;
+    M::recover(u, bc, yr, s2, b2, ps, pg);
     v[0] = m1;
     v[1] = M::sub(M::add(M::mul(m1, vx), ps), M::mul(bx, bx));
     v[2] = M::sub(M::mul(m2, vx), M::mul(by, bx));
     v[3] = M::sub(M::mul(m3, vx), M::mul(bz, bx));
     const float dot = M::add(M::add(M::mul(bx, m1), M::mul(by, m2)), M::mul(bz, m3));
     v[4] = M::sub(M::mul(M::add(e, ps), vx), M::divy(M::mul(bx, dot), r, yr));
-    p = M::sub(ps, 0.5f * b2);                             // mhdflux.c:39-42, one rounding
+    p = pg;
     const float a = M::divy(M::add(b2, M::mul(kGamma, p)), r, yr);
     cs = M::speed(fabsf(vx), fabsf(a));
 }

@@ -73,7 +73,7 @@ extern "C" {
 
 int mhdgpu_set_math(int mode)
 {
-    if (mode != MHD_MATH_FAITHFUL && mode != MHD_MATH_FAST) {
+    if (mode != MHD_MATH_FAITHFUL && mode != MHD_MATH_FAST && mode != MHD_MATH_FP64P) {
         set_last_error("mhdgpu_set_math: unknown mode");
         return -1;
     }
@@ -122,7 +122,7 @@ int mhdgpu_autotune(int nx, int ny, int nz, int math)
         set_last_error("mhdgpu_autotune: bad box");
         return MHD_ERR_ARG;
     }
-    if (math != MHD_MATH_FAITHFUL && math != MHD_MATH_FAST) {
+    if (math != MHD_MATH_FAITHFUL && math != MHD_MATH_FAST && math != MHD_MATH_FP64P) {
         set_last_error("mhdgpu_autotune: unknown math mode");
         return MHD_ERR_ARG;
     }

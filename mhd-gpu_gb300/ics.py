@@ -173,6 +173,128 @@ def ensemble(nbox=64, seed=0, sizes=(32, 48, 64, 96, 128), amp_range=(1e-4, 1e-1
     return out
 
 
+def blast(n=256, r0=0.1, p_in=100.0, p_out=0.1, rho0=1.0, b0=(10.0 / np.sqrt(2.0), 10.0 / np.sqrt(2.0), 0.0),
+          dtype=np.float32, ny=None, nz=None):
+    """Spherical MHD blast: gas pressure p_in inside radius r0*L of the box
+    centre and p_out outside, rho = rho0 and v = 0 everywhere, uniform
+    B = b0 (default (1,1,0)/sqrt(2)*10: beta = 2 p_out/B^2 = 0.002 outside).
+    L = n (unit cells); the radius is measured between cell centres."""
+    nx = n
+    ny = n if ny is None else ny
+    nz = n if nz is None else nz
+    kk, jj, ii = np.meshgrid(np.arange(nz) + 0.5, np.arange(ny) + 0.5, np.arange(nx) + 0.5, indexing="ij")
+    r = np.sqrt((ii - nx / 2) ** 2 + (jj - ny / 2) ** 2 + (kk - nz / 2) ** 2)
+    rho = np.full((nz, ny, nx), rho0)
+    p = np.where(r < r0 * nx, p_in, p_out)
+    m = np.zeros((3, nz, ny, nx))
+    b = np.broadcast_to(np.asarray(b0, dtype=np.float64)[:, None, None, None], (3, nz, ny, nx)).copy()
+    e = _energy(rho, m, b, p)
+    return _pack(rho, m, e, b, dtype)
+
+
+FORTRAN_ICS = ("sound", "cp_alfven", "alfven", "magnetic", "magnetosonic", "oblique")
+
+
+def fortran_ic(kind, nx, ny=1, nz=None):
+    """The analytic initial states of the Fortran original's init
+    (OpenMP/mhd.f90:130-247), restated in float32 (its default real kind):
+    1-based x index i, phase 2*3.14159*i/nx in float, cshift(a,-1,dim)
+    = roll by +1 along dim.
+
+      sound:        rho = 1 + 1e-4 sin, m_x = 1e-4 sin on the (j,k) = (1,1) line,
+                    p0 = 3/5, B = (1,0,0)            (mhd.f90:136-146)
+      cp_alfven:    circularly polarised Alfven wave, amplitude 0.1, B0 = x
+                                                      (mhd.f90:147-162)
+      alfven:       linear Alfven wave, m_y = 0.1 sin, b_y = -m_y averaged
+                    with its x-1 neighbour            (mhd.f90:164-179)
+      magnetic:     m_x = 1e-3 sin, b_y = 1 + m_x, rho = b_y (mhd.f90:180-192)
+      magnetosonic: p0 = 3/10, b_y = (1 + m_x)/sqrt 2, rho = 1 + m_x,
+                    m_x = 1e-4 sin                    (mhd.f90:193-206)
+      oblique:      the wave along (1,0,1) that the original ends on
+                                                      (mhd.f90:222-246)
+    Returns flat float32 (u, b) in the reference layout."""
+    f32 = np.float32
+    nz = nx if nz is None else nz
+    if kind not in FORTRAN_ICS:
+        raise ValueError(f"unknown initial state {kind!r}; one of {FORTRAN_ICS}")
+    u = np.zeros((5, nz, ny, nx), dtype=f32)      # [field, k, j, i]
+    b = np.zeros((3, nz, ny, nx), dtype=f32)
+    two_pi = f32(2) * f32(3.14159)
+    ph = (two_pi * np.arange(1, nx + 1, dtype=f32) / f32(nx)).astype(f32)    # along x
+    sin_x, cos_x = np.sin(ph).astype(f32), np.cos(ph).astype(f32)
+    half = f32(2)
+
+    def ke(u):
+        return ((u[1] ** 2 + u[2] ** 2 + u[3] ** 2) / u[0] / half).astype(f32)
+
+    def me(b):
+        return ((b[0] ** 2 + b[1] ** 2 + b[2] ** 2) / half).astype(f32)
+
+    if kind == "sound":
+        p0 = f32(3.0) / f32(5.0)
+        b[0] = 1
+        u[0] = 1
+        u[4] = f32(1.5) * p0
+        u[1, 0, 0, :] = f32(0.0001) * sin_x
+        u[0, 0, 0, :] = u[0, 0, 0, :] + u[1, 0, 0, :]
+        u[4] = u[4] + me(b) + (u[1] ** 2 / u[0] / half).astype(f32)
+        u[4, 0, 0, :] = u[4, 0, 0, :] + p0 * u[1, 0, 0, :] * f32(5.0) / f32(3.0) / (f32(2.0) / f32(3.0))
+    elif kind == "cp_alfven":
+        b[0] = 1
+        u[0] = 1
+        u[4] = f32(0.1)
+        u[2] = f32(0.1) * sin_x
+        u[3] = f32(0.1) * cos_x
+        b[1] = -u[2]
+        b[2] = -u[3]
+        b[1] = (b[1] + np.roll(b[1], 1, axis=1)) / half      # cshift(.,-1,2): along y
+        b[2] = (b[2] + np.roll(b[2], 1, axis=0)) / half      # cshift(.,-1,3): along z
+        u[4] = u[4] + me(b) + ke(u)
+    elif kind == "alfven":
+        b[0] = 1
+        u[0] = 1
+        u[4] = f32(0.001)
+        u[2] = f32(0.1) * sin_x
+        b[1] = -u[2]
+        b[1] = (b[1] + np.roll(b[1], 1, axis=2)) / half      # cshift(.,-1,1): along x
+        u[4] = u[4] + me(b) + (u[2] ** 2 / u[0] / half).astype(f32)
+    elif kind == "magnetic":
+        b[1] = 1
+        u[0] = 1
+        u[4] = f32(0.000000001)
+        u[1] = f32(0.001) * sin_x
+        b[1] = b[1] + u[1]
+        u[0] = b[1]
+        u[4] = u[4] + me(b) + ke(u)
+    elif kind == "magnetosonic":
+        p0 = f32(3.0) / f32(5.0) / f32(2.0)
+        r2 = f32(np.sqrt(f32(2.0)))
+        b[1] = f32(1.0) / r2
+        u[0] = 1
+        u[4] = p0 * f32(1.5)
+        u[1] = f32(0.0001) * sin_x
+        b[1] = b[1] + u[1] / r2
+        u[0] = u[0] + u[1]
+        u[4] = u[4] + me(b) + ke(u)
+        u[4] = u[4] + p0 * u[1] * f32(5.0) / f32(3.0) / (f32(2.0) / f32(3.0))
+    else:  # oblique
+        r2 = f32(np.sqrt(f32(2.0)))
+        phk = (two_pi * np.arange(1, nz + 1, dtype=f32) / f32(nz)).astype(f32)
+        p = (ph[None, None, :] + phk[:, None, None]).astype(f32) * np.ones((1, ny, 1), dtype=f32)
+        sp, cp = np.sin(p).astype(f32), np.cos(p).astype(f32)
+        u[0] = 1
+        u[2] = f32(-0.1) * cp
+        u[1] = f32(-0.1) * sp / r2
+        u[3] = f32(0.1) * sp / r2
+        b[1] = f32(0.1) * cp
+        b[0] = (f32(1.0) + f32(0.1) * sp) / r2
+        b[2] = (f32(1.0) - f32(0.1) * sp) / r2
+        u[4] = f32(1.5) + f32(0.01)
+    uu = np.ascontiguousarray(np.moveaxis(u, 0, -1)).ravel()
+    bb = np.ascontiguousarray(np.moveaxis(b, 0, -1)).ravel()
+    return uu.astype(np.float32), bb.astype(np.float32)
+
+
 def random_state(nx, ny, nz, seed=0, dtype=np.float32, amp=0.3, bmean=(0.3, 0.1, -0.2)):
     """Seeded random but physical state (positive density and pressure) used by
     the per-subroutine parity tests."""

@@ -39,12 +39,16 @@ EXPORTS = [
     "mhdgpu_run_host", "mhdgpu_set_math", "mhdgpu_set_tile", "mhdgpu_get_tile",
     "mhdgpu_autotune", "mhdgpu_profiler_create", "mhdgpu_profiler_destroy",
     "mhdgpu_profiler_attach", "mhdgpu_profiler_reset", "mhdgpu_profiler_summary",
+    "mhdgpu_diagnostics_scratch_bytes", "mhdgpu_diagnostics",
+    "mhdgpu_read_state", "mhdgpu_write_state", "mhdgpu_write_result", "mhdgpu_write_check",
     "mhdgpu_batch_workspace_bytes", "mhdgpu_batch_create", "mhdgpu_batch_destroy",
     "mhdgpu_batch_advance", "mhdgpu_batch_read_clocks", "mhdgpu_batch_set_schedule",
     "mhdgpu_batch_get_schedule", "mhdgpu_batch_tune",
     # include/mhdgpu_compat.h
     "fluidx", "advectbyzx", "transpose12", "transpose13", "calcfl", "copy_matrix",
     "mhdgpu_compat_status",
+    # include/mhdgpu_fortran.h
+    "fluidx_", "advectbyzx_", "transpose12_", "transpose13_", "cfl_",
 ]
 
 
@@ -99,6 +103,12 @@ def lib() -> C.CDLL:
             "mhdgpu_profiler_attach": (I, [P]),
             "mhdgpu_profiler_reset": (I, [P]),
             "mhdgpu_profiler_summary": (I, [P, I, P, P, P]),
+            "mhdgpu_diagnostics_scratch_bytes": (S, [I, I, I]),
+            "mhdgpu_diagnostics": (I, [P, P, I, I, I, P, P, P]),
+            "mhdgpu_read_state": (I, [C.c_char_p, P, P, I, I, I]),
+            "mhdgpu_write_state": (I, [C.c_char_p, P, P, I, I, I]),
+            "mhdgpu_write_result": (I, [C.c_char_p, C.c_char_p, P, P, I, I, I]),
+            "mhdgpu_write_check": (I, [C.c_char_p, P, P, I, I, I]),
             "mhdgpu_batch_workspace_bytes": (S, [I, P]),
             "mhdgpu_batch_create": (I, [P, I, P, P, P, D, I, P]),
             "mhdgpu_batch_destroy": (I, [P]),
@@ -108,6 +118,7 @@ def lib() -> C.CDLL:
             "mhdgpu_batch_get_schedule": (I, [P, I, P, P]),
             "mhdgpu_batch_tune": (I, [P, P]),
             "calcfl": (F, [P, P, P, P, P]),
+            "cfl_": (F, [P, P, P, P, P]),
             "mhdgpu_compat_status": (I, []),
         }
         for name, (res, args) in sig.items():
@@ -227,6 +238,7 @@ def run_host(u, b, nx, ny, nz, cfl_number=0.9, cfl_mode=MHD_CFL_C, t=0.0, tf=0.0
 
 MHD_MATH_FAITHFUL = 0
 MHD_MATH_FAST = 1
+MHD_MATH_FP64P = 2
 
 
 def set_math(mode: int) -> int:
@@ -304,6 +316,54 @@ class Profiler:
             self.close()
         except Exception:
             pass
+
+
+def _host_f32(a, n):
+    import numpy as np
+    if not (isinstance(a, np.ndarray) and a.dtype == np.float32 and a.flags.c_contiguous and a.size == n):
+        raise ValueError("expected a C-contiguous float32 numpy array of %d elements" % n)
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def read_state(path, nx, ny, nz):
+    """The reference's init file (Heterogeneous_MHD/C/init.c:33-66) -> (u, b) numpy."""
+    import numpy as np
+    n = nx * ny * nz
+    u = np.empty(5 * n, dtype=np.float32)
+    b = np.empty(3 * n, dtype=np.float32)
+    _check(lib().mhdgpu_read_state(os.fsencode(path), _host_f32(u, 5 * n), _host_f32(b, 3 * n), nx, ny, nz))
+    return u, b
+
+
+def write_state(path, u, b, nx, ny, nz):
+    n = nx * ny * nz
+    _check(lib().mhdgpu_write_state(os.fsencode(path), _host_f32(u, 5 * n), _host_f32(b, 3 * n), nx, ny, nz))
+
+
+def write_result(path_u, path_b, u, b, nx, ny, nz):
+    n = nx * ny * nz
+    _check(lib().mhdgpu_write_result(os.fsencode(path_u), os.fsencode(path_b), _host_f32(u, 5 * n),
+                                     _host_f32(b, 3 * n), nx, ny, nz))
+
+
+def write_check(prefix, u, b, nx, ny, nz):
+    n = nx * ny * nz
+    _check(lib().mhdgpu_write_check(os.fsencode(prefix), _host_f32(u, 5 * n), _host_f32(b, 3 * n), nx, ny, nz))
+
+
+DIAG_NAMES = ("mass", "m_x", "m_y", "m_z", "energy", "max_div_b", "min_p", "cells_p_nonpositive")
+
+
+def diagnostics(u, b, nx, ny, nz, stream=None) -> dict:
+    """FP64 totals, max |div B|, min p and the count of p <= 0 cells of a device
+    state (mhdgpu_diagnostics); synchronises the stream to return host values."""
+    import torch
+    out = torch.empty(8, dtype=torch.float64, device=u.device)
+    scr = torch.empty(int(lib().mhdgpu_diagnostics_scratch_bytes(nx, ny, nz)), dtype=torch.uint8,
+                      device=u.device)
+    _check(lib().mhdgpu_diagnostics(_p(u), _p(b), nx, ny, nz, _p(out), _p(scr), _stream(stream)))
+    vals = out.cpu().tolist()
+    return dict(zip(DIAG_NAMES, vals))
 
 
 def batch_workspace_bytes(dims) -> int:

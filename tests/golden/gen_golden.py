@@ -57,10 +57,24 @@ def subroutines(R, u, b, dims, dt):
     return out
 
 
+def write_digest(ref):
+    """sha256 of the shipped init file: pins the state-file writer to the
+    reference's own bytes without copying the file."""
+    import hashlib
+    path = os.path.join(ref, "data", "source_init_alfvenlinear_16cube.dat")
+    raw = open(path, "rb").read()
+    with open(os.path.join(HERE, "alfven16_dat_sha256.txt"), "w") as f:
+        f.write(f"{hashlib.sha256(raw).hexdigest()} {len(raw)}\n")
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default=os.environ.get("MHD_REFERENCE", "/root/reference"))
+    ap.add_argument("--only-digest", action="store_true")
     args = ap.parse_args()
+    write_digest(args.ref)
+    if args.only_digest:
+        return
     R = O.reference("f32")
     R64 = O.reference("f64")
 

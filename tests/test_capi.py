@@ -11,7 +11,7 @@ REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 def _declared_functions():
     names = []
-    for h in ("mhdgpu.h", "mhdgpu_compat.h"):
+    for h in ("mhdgpu.h", "mhdgpu_compat.h", "mhdgpu_fortran.h"):
         src = open(os.path.join(REPO, "include", h)).read()
         src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
         for m in re.finditer(r"^\s*[A-Za-z_][\w\s\*]*?\b([A-Za-z_]\w*)\s*\(", src, flags=re.M):
@@ -134,3 +134,17 @@ def test_batch_workspace_bytes(L):
     assert 8 * cells < ws < 8 * cells + 4096
     assert mhdgpu.batch_workspace_bytes([(8, 8, 0)]) == 0
     assert mhdgpu.batch_workspace_bytes([(8, 300, 8)]) == 0
+
+
+def test_diagnostics_arguments_without_a_gpu(L):
+    import mhdgpu
+    P = C.c_void_p
+    fake = P(0x1000)
+    assert L.mhdgpu_diagnostics_scratch_bytes(0, 4, 4) == 0
+    assert 0 < L.mhdgpu_diagnostics_scratch_bytes(512, 512, 512) <= 40 * 1024
+    assert L.mhdgpu_diagnostics(fake, fake, 0, 4, 4, fake, fake, None) == mhdgpu.MHD_ERR_ARG
+    assert L.mhdgpu_diagnostics(None, fake, 4, 4, 4, fake, fake, None) == mhdgpu.MHD_ERR_ARG
+    assert L.mhdgpu_diagnostics(fake, fake, 4, 4, 4, fake, None, None) == mhdgpu.MHD_ERR_ARG
+    assert L.mhdgpu_set_math(mhdgpu.MHD_MATH_FP64P) == mhdgpu.MHD_MATH_FAITHFUL
+    assert L.mhdgpu_set_math(mhdgpu.MHD_MATH_FAITHFUL) == mhdgpu.MHD_MATH_FP64P
+    assert L.mhdgpu_set_math(3) == -1

@@ -12,10 +12,12 @@ from util import bits_equal
 
 pytestmark = pytest.mark.gpu
 
-# one box per team class of the batched kernel along some axis: n < 32, 32,
-# 33..63, 64, 65..127, 96, 128, 129..256 (x, y or z pencils)
+# every team class of the batched kernel, along x (contiguous pencils) and
+# along y or z (pencils across memory): n = 32, 48, 64, 96, 128, other n < 64,
+# other n < 128, n <= 256, and degenerate boxes
 CLASS_BOXES = [(8, 16, 24), (32, 48, 20), (64, 40, 12), (96, 8, 16), (130, 12, 8), (16, 200, 8),
-               (8, 8, 128), (100, 16, 10), (5, 7, 9), (1, 4, 3)]
+               (8, 8, 128), (100, 16, 10), (5, 7, 9), (1, 4, 3), (16, 96, 8), (48, 32, 64),
+               (12, 128, 6)]
 
 
 def dev(a):
@@ -169,10 +171,31 @@ def test_batch_graph_replay(gpu):
     _same(got, ref)
 
 
-def test_batch_fast_math_equals_per_box(gpu):
+def test_batch_fast_math_matches_per_box(gpu):
+    """The fast policy lets the compiler contract multiply-adds, and the
+    contraction can differ between the single-box and the batched kernels in
+    the last bit; the faithful policy (the other tests) is bit-reproducible.
+    Here: agreement within 1e-5 per field and in dt."""
+    from util import field_errors
     dims = [(32, 48, 20), (100, 16, 10), (8, 8, 128)]
     states = _states(dims, seed=8)
     prev = gpu.set_math(gpu.MHD_MATH_FAST)
+    try:
+        ref = _per_box(gpu, states, dims, 3, 0.7)
+        got = _batched(gpu, states, dims, 3, 0.7)
+    finally:
+        gpu.set_math(prev)
+    for (u1, b1, c1), (u2, b2, c2) in zip(got, ref):
+        assert max(field_errors(u1, u2, 5)) < 1e-5 and max(field_errors(b1, b2, 3)) < 1e-5
+        assert c1.iter == c2.iter and abs(c1.dt - c2.dt) <= 1e-5 * abs(c2.dt)
+
+
+def test_batch_fp64_pressure_equals_per_box(gpu):
+    """The FP64 pressure-recovery policy on low-beta boxes: bit for bit."""
+    import ics
+    dims = [(32, 24, 16), (48, 32, 20)]
+    states = [ics.blast(d[0], ny=d[1], nz=d[2]) for d in dims]
+    prev = gpu.set_math(gpu.MHD_MATH_FP64P)
     try:
         ref = _per_box(gpu, states, dims, 3, 0.7)
         got = _batched(gpu, states, dims, 3, 0.7)
@@ -194,4 +217,6 @@ def test_batch_ensemble_workload_sample(gpu):
     _same(got, ref)
     for (u, b, c), e in zip(got, ens):
         assert np.isfinite(u).all() and c.health & (gpu.MHD_HEALTH_NONFINITE | gpu.MHD_HEALTH_DENSITY) == 0
-        assert ics.div_b(b, *e["dims"]) < 2 * ics.div_b(e["b"], *e["dims"]) + 1e-6
+        # round-off of the face updates: a few ulps of |B| per step
+        bound = 2 * ics.div_b(e["b"], *e["dims"]) + 5 * 16 * 2.0 ** -24 * float(np.abs(b).max())
+        assert ics.div_b(b, *e["dims"]) < bound

@@ -1,0 +1,182 @@
+"""Precision studies on the GPU against the FP64 oracle, through the C ABI.
+
+  - mhdgpu_diagnostics (FP64 totals, max |div B|, min p) against numpy in
+    float64 on the same state;
+  - the FP64 pressure-recovery policy (MHD_MATH_FP64P): bit-identical to the
+    faithful policy where beta >= 0.1, and on the low-beta blast compared with
+    the faithful FP32 run and the FP64 oracle on positivity, energy
+    conservation and max |div B|;
+  - the turbulent start: per-field error of the FP32 step against the FP64
+    oracle fed the same dt sequence.
+
+The FP64 oracle runs replay the GPU run's dt sequence (dt_log) so that the
+comparison isolates the arithmetic precision from the CFL's rounding.
+Studies marked `slow` run the full-size configurations and are skipped unless
+MHDGPU_SLOW=1.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from util import U_FIELDS, B_FIELDS, bits_equal, field_errors
+
+pytestmark = pytest.mark.gpu
+SLOW = os.environ.get("MHDGPU_SLOW") == "1"
+
+
+def dev(a):
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def host(t):
+    import torch
+    torch.cuda.synchronize()
+    return t.cpu().numpy()
+
+
+def gas_pressure(u, b, nx, ny, nz):
+    """p = (gamma-1)(E - m^2/2rho - Bc^2/2) in float64, Bc face -> centre."""
+    g = float(np.float32(5.0 / 3.0))
+    uu = np.asarray(u, dtype=np.float64).reshape(nz, ny, nx, 5)
+    bb = np.asarray(b, dtype=np.float64).reshape(nz, ny, nx, 3)
+    cx = 0.5 * (bb[..., 0] + np.roll(bb[..., 0], -1, axis=2))
+    cy = 0.5 * (bb[..., 1] + np.roll(bb[..., 1], -1, axis=1))
+    cz = 0.5 * (bb[..., 2] + np.roll(bb[..., 2], -1, axis=0))
+    q = (uu[..., 1] ** 2 + uu[..., 2] ** 2 + uu[..., 3] ** 2) / uu[..., 0]
+    return (g - 1.0) * (uu[..., 4] - 0.5 * q - 0.5 * (cx ** 2 + cy ** 2 + cz ** 2))
+
+
+def gpu_run(gpu, u, b, dims, nsteps, cfl, math, path=1):
+    """nsteps on the device under a math policy; returns (u, b, dt_log, clock,
+    diagnostics before, diagnostics after)."""
+    import torch
+    prev = gpu.set_math(math)
+    try:
+        du, db = dev(u), dev(b)
+        d0 = gpu.diagnostics(du, db, *dims)
+        work = torch.empty(gpu.step_workspace_bytes(*dims, path), dtype=torch.uint8, device="cuda")
+        clock = gpu.new_clock()
+        log = torch.zeros(nsteps, dtype=torch.float32, device="cuda")
+        gpu.advance(du, db, *dims, nsteps, cfl, 0, 0.0, clock, log, work, path)
+        d1 = gpu.diagnostics(du, db, *dims)
+        return host(du), host(db), host(log), gpu.read_clock(clock), d0, d1
+    finally:
+        gpu.set_math(prev)
+
+
+def oracle64_replay(oracle_lib, u, b, dims, dts, threads=None):
+    """The FP64 oracle from the same initial state with a given dt sequence."""
+    O = oracle_lib.oracle("f64")
+    if threads:
+        oracle_lib.set_threads(threads)
+    uu = np.asarray(u, dtype=np.float64).copy()
+    bb = np.asarray(b, dtype=np.float64).copy()
+    wu, wb = np.empty_like(uu), np.empty_like(bb)
+    for dt in dts:
+        O.step(uu, bb, *dims, np.float64(dt), wu, wb)
+    return uu, bb
+
+
+def test_diagnostics_match_numpy(gpu):
+    import ics
+    dims = (24, 16, 20)
+    u, b = ics.random_state(*dims, seed=12, amp=0.3)
+    d = gpu.diagnostics(dev(u), dev(b), *dims)
+    uu = np.asarray(u, dtype=np.float64).reshape(-1, 5)
+    for i, k in enumerate(("mass", "m_x", "m_y", "m_z", "energy")):
+        ref = uu[:, i].sum()
+        assert abs(d[k] - ref) <= 1e-12 * max(1.0, np.abs(uu[:, i]).sum()), k
+    assert d["max_div_b"] == pytest.approx(ics.div_b(b, *dims), rel=1e-12)
+    p = gas_pressure(u, b, *dims)
+    assert d["min_p"] == pytest.approx(p.min(), rel=1e-12)
+    assert d["cells_p_nonpositive"] == float((p <= 0).sum())
+    d2 = gpu.diagnostics(dev(u), dev(b), *dims)
+    assert d2 == d          # fixed reduction order: repeatable bit for bit
+
+
+def test_fp64_pressure_equals_faithful_at_high_beta(gpu):
+    """Where beta >= 0.1 the FP64 recovery is not taken: same bits."""
+    import ics
+    dims = (32, 16, 24)
+    u, b = ics.turbulence(*dims, seed=4, mach=0.3, b_mean=0.3, db_rms=0.3)
+    bb = np.asarray(b, dtype=np.float64).reshape(dims[2], dims[1], dims[0], 3)
+    bc2 = sum((0.5 * (bb[..., a] + np.roll(bb[..., a], -1, axis=2 - a))) ** 2 for a in range(3))
+    assert (2 * gas_pressure(u, b, *dims) / bc2).min() > 0.5   # beta far above 0.1
+    a = gpu_run(gpu, u, b, dims, 3, 0.7, gpu.MHD_MATH_FAITHFUL)
+    c = gpu_run(gpu, u, b, dims, 3, 0.7, gpu.MHD_MATH_FP64P)
+    assert bits_equal(a[0], c[0]) and bits_equal(a[1], c[1])
+
+
+def _blast_study(gpu, oracle_lib, n, nsteps, threads=None):
+    import ics
+    dims = (n, n, n)
+    u, b = ics.blast(n)
+    res = {}
+    for name, math in (("fp32", gpu.MHD_MATH_FAITHFUL), ("fp64_pressure", gpu.MHD_MATH_FP64P)):
+        gu, gb, dts, clk, d0, d1 = gpu_run(gpu, u, b, dims, nsteps, 0.7, math)
+        ru, rb = oracle64_replay(oracle_lib, u, b, dims, dts, threads)
+        p, p64 = gas_pressure(gu, gb, *dims), gas_pressure(ru, rb, *dims)
+        res[name] = {
+            "health": clk.health, "min_p": d1["min_p"], "cells_p_nonpositive": d1["cells_p_nonpositive"],
+            "energy_drift": abs(d1["energy"] - d0["energy"]) / abs(d0["energy"]),
+            "max_div_b": d1["max_div_b"], "oracle64_min_p": float(p64.min()),
+            "p_err_vs_fp64_over_p_out": float(np.abs(p - p64).max() / 0.1),
+            "field_err_vs_fp64": dict(zip(U_FIELDS + B_FIELDS,
+                                          field_errors(gu, ru, 5) + field_errors(gb, rb, 3))),
+        }
+    return res
+
+
+def test_lowbeta_blast_fp64_pressure_small(gpu, oracle_lib):
+    """32^3 blast (beta = 0.002 outside), 20 steps: both policies stay finite
+    with rho > 0 and conserve energy to round-off; the FP64 recovery's gas
+    pressure is at least as close to the FP64 oracle's as the FP32 one."""
+    res = _blast_study(gpu, oracle_lib, 32, 20)
+    print(res)
+    for name, r in res.items():
+        assert r["health"] & (gpu.MHD_HEALTH_NONFINITE | gpu.MHD_HEALTH_DENSITY) == 0, name
+        assert r["energy_drift"] < 1e-6, name
+        assert r["max_div_b"] < 1e-4, name
+    assert res["fp64_pressure"]["p_err_vs_fp64_over_p_out"] <= res["fp32"]["p_err_vs_fp64_over_p_out"] * 1.05
+
+
+@pytest.mark.slow
+@pytest.mark.skipif(not SLOW, reason="full-size study: set MHDGPU_SLOW=1")
+def test_lowbeta_blast_study_128(gpu, oracle_lib):
+    res = _blast_study(gpu, oracle_lib, 128, 300, threads=os.cpu_count())
+    print("LOWBETA_STUDY", res)
+    for r in res.values():
+        assert r["health"] & (gpu.MHD_HEALTH_NONFINITE | gpu.MHD_HEALTH_DENSITY) == 0
+
+
+def _turbulence_study(gpu, oracle_lib, n, nsteps, threads=None):
+    import ics
+    dims = (n, n, n)
+    u, b = ics.turbulence(n, seed=7, mach=0.5, b_mean=0.3)
+    out = {}
+    for name, math in (("faithful", gpu.MHD_MATH_FAITHFUL), ("fast", gpu.MHD_MATH_FAST)):
+        gu, gb, dts, clk, d0, d1 = gpu_run(gpu, u, b, dims, nsteps, 0.7, math)
+        ru, rb = oracle64_replay(oracle_lib, u, b, dims, dts, threads)
+        out[name] = dict(zip(U_FIELDS + B_FIELDS, field_errors(gu, ru, 5) + field_errors(gb, rb, 3)))
+        out[name]["energy_drift"] = abs(d1["energy"] - d0["energy"]) / abs(d0["energy"])
+        out[name]["max_div_b"] = d1["max_div_b"]
+    return out
+
+
+def test_turbulence_fp32_vs_fp64_small(gpu, oracle_lib):
+    """48^3 turbulent start (k^-2 velocity at rms Mach 0.5, k^-3 potential,
+    mean field 0.3), 10 steps: the FP32 step is within 1e-5 per field of the
+    FP64 oracle on the same dt sequence."""
+    out = _turbulence_study(gpu, oracle_lib, 48, 10)
+    print(out)
+    for f in U_FIELDS + B_FIELDS:
+        assert out["faithful"][f] < 1e-5, (f, out["faithful"][f])
+
+
+@pytest.mark.slow
+@pytest.mark.skipif(not SLOW, reason="full-size study: set MHDGPU_SLOW=1")
+def test_turbulence_precision_study_256(gpu, oracle_lib):
+    out = _turbulence_study(gpu, oracle_lib, 256, 50, threads=os.cpu_count())
+    print("TURBULENCE_STUDY", out)
