@@ -347,7 +347,7 @@ def single_box(n, K, W, stream, flush, world, dev, tune, math_mode):
     return res
 
 
-def ensemble_bench(ens, K, W, stream, flush, world, dev, tune, sampler):
+def ensemble_bench(ens, K, W, stream, flush, world, dev, tune):
     """Batched ensemble vs box-by-box loops; e2e through mhdgpu_batch_* with
     the state uploaded from and downloaded to pinned host memory every step."""
     import numpy as np
@@ -363,7 +363,6 @@ def ensemble_bench(ens, K, W, stream, flush, world, dev, tune, sampler):
         bt.advance(1, stream=stream)
 
     g = capture(step, stream, 2)
-    t_w0 = time.time()
     secs, wall = timed_replays(g.replay, K, W, stream, flush, world)
     del g
     summ = profiled(step, max(3, min(K, 20)), stream, flush)
@@ -452,6 +451,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--math", default="faithful", choices=["faithful", "fast"])
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuners (default tiles)")
+    ap.add_argument("--headline-only", action="store_true",
+                    help="time the headline path only (no secondary paths, e2e or CPU baseline); "
+                         "for profiler captures")
     args = ap.parse_args()
     n, K, W = args.n, args.steps, max(3, args.warmup)
     ens_mode = args.workload == "ensemble64"
@@ -516,10 +518,37 @@ def main():
     time.sleep(0.3)
     tune = not args.no_tune
 
+    if args.headline_only:
+        if ens_mode:
+            ens = ics.ensemble(**ENSEMBLE)
+            boxes = [(torch.from_numpy(e["u"]).to(dev), torch.from_numpy(e["b"]).to(dev), e["dims"]) for e in ens]
+            bt = mhdgpu.Batch(boxes, cfl_number=CFL, cfl_mode=mhdgpu.MHD_CFL_C)
+            if tune:
+                bt.tune(stream=stream)
+            g = capture(lambda: bt.advance(1, stream=stream), stream, 2)
+            cells = sum(e["dims"][0] * e["dims"][1] * e["dims"][2] for e in ens)
+        else:
+            u0, b0 = ics.alfven_oblique(n)
+            du, db = torch.from_numpy(u0).to(dev), torch.from_numpy(b0).to(dev)
+            work = torch.empty(mhdgpu.step_workspace_bytes(n, n, n, 1), dtype=torch.uint8, device=dev)
+            clock = mhdgpu.new_clock(device=dev)
+            if tune:
+                mhdgpu.autotune(n, n, n, math_mode)
+            g = capture(lambda: mhdgpu.advance(du, db, n, n, n, 1, CFL, 0, 0.0, clock, None, work, 1),
+                        stream, 2)
+            cells = n ** 3
+        secs, wall = timed_replays(g.replay, K, W, stream, flush, world)
+        sampler.stop()
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": world * cells * K / secs, "unit": UNIT,
+                              "n_gpus": world, "steps": K, "warmup": W, "ms_per_step": secs / K * 1e3,
+                              "config": config, "note": "--headline-only: no secondary measurements"}))
+        return
+
     sb = single_box(n, K, W, stream, flush, world, dev, tune, math_mode)
     if ens_mode:
         ens = ics.ensemble(**ENSEMBLE)
-        eb = ensemble_bench(ens, K, W, stream, flush, world, dev, tune, sampler)
+        eb = ensemble_bench(ens, K, W, stream, flush, world, dev, tune)
         sampler.stop()
         clocks = sampler.summary(*eb["wall"])
         value, ms_step = eb["value"], eb["ms_per_step"]

@@ -314,6 +314,13 @@ int mhdgpu_batch_get_schedule(const mhdgpu_batch *bt, int axis, int *threads, in
  * restores the boxes' state and clocks.  Allocates a snapshot of the state
  * for the duration; synchronises.  Not under stream capture. */
 int mhdgpu_batch_tune(mhdgpu_batch *bt, mhdgpu_stream_t stream);
+/* Failure-path test hook: from the next step on, the first dependency wait of
+ * box 0 in the first sweep waits for one item more than exist, so it gives up
+ * after its limit (about two seconds): the box's health gets MHD_HEALTH_STALL,
+ * the batch's later waits return at once, the launches drain and
+ * mhdgpu_batch_read_clocks returns MHD_ERR_TIMEOUT.  The batch's state is then
+ * invalid; the context stays usable. */
+int mhdgpu_batch_inject_stall(mhdgpu_batch *bt);
 
 /* ------------------------------------------------------------------------
  * Profiler: per-kernel-class device time from CUDA events.  While a profiler

@@ -69,6 +69,19 @@ constexpr int kThreadChoices[3] = {64, 128, 256};
 
 }  // namespace
 
+// one persistent launch: the boxes of one team class in one sweep
+struct BatchGroup {
+    int sweep = 0, cls = 0, nb = 0;
+    std::vector<int> boxes;       // batch indices of the group's boxes
+    size_t off_args = 0;          // first entry in d_fa / d_aa
+    size_t off_start = 0;         // first entry in d_start (3 nb + 1)
+    size_t off_group = 0;         // first entry in d_group (3 nb)
+    size_t off_ctr = 0;           // claim word, then 3 nb completion words, in d_ctr
+    long long cells = 0, items = 0;
+    size_t smem = 0;
+    int grid = 1;
+};
+
 struct mhdgpu_batch {
     int nbox = 0;
     int device = 0, num_sms = 0;
@@ -79,24 +92,33 @@ struct mhdgpu_batch {
     mhdgpu_clock *d_clk = nullptr;
     float *d_scr = nullptr;
     float *d_tf = nullptr;
-    // counters: 6 claims, then 6 x 3*nbox completion counts; then the abort word
-    unsigned *d_ctr = nullptr;
+    std::vector<BatchGroup> groups;     // ordered by sweep
+    int gbegin[7] = {};                 // groups of sweep s: [gbegin[s], gbegin[s+1])
+    std::vector<FluidxArgs> fa;         // 6 * nbox entries (host: they travel in the launches)
+    std::vector<AdvectArgs> aa;
+    long long *d_start = nullptr;
+    int *d_group = nullptr;
+    unsigned *d_ctr = nullptr;          // the groups' counters, then the abort word
     int nctr = 0;
     unsigned *d_abort = nullptr;
-    long long *d_start = nullptr;       // 6 x (3*nbox + 1)
-    int *d_group = nullptr;             // 6 x 3*nbox
     long long *d_cfl_start = nullptr;   // nbox + 1
     long long cfl_total = 0;
-    long long total[6] = {};
     int threads[3] = {256, 256, 256};
-    int cps[3] = {3, 3, 3};             // requested CTAs per SM
-    int grid[6] = {};
-    size_t smem[3] = {};
+    int cps[3] = {8, 8, 8};             // CTAs per SM cap (the occupancy limits it further)
+    unsigned stall_extra = 0;           // mhdgpu_batch_inject_stall
+    ClassWork work{};                   // parameter block of one launch (filled per launch)
+    cudaStream_t side[kBatchClasses] = {};
+    cudaEvent_t fork = nullptr, join[kBatchClasses] = {};
 
     ~mhdgpu_batch()
     {
         cudaFree(d_box); cudaFree(d_clk); cudaFree(d_scr); cudaFree(d_tf);
         cudaFree(d_ctr); cudaFree(d_start); cudaFree(d_group); cudaFree(d_cfl_start);
+        for (int i = 0; i < kBatchClasses; ++i) {
+            if (side[i]) cudaStreamDestroy(side[i]);
+            if (join[i]) cudaEventDestroy(join[i]);
+        }
+        if (fork) cudaEventDestroy(fork);
     }
 };
 
@@ -133,80 +155,143 @@ bool dims_ok(int nbox, const int *dims)
 
 long long cells_of(const int *d) { return (long long)d[0] * d[1] * d[2]; }
 
-int occupancy(bool rows, int threads, size_t smem)
+int occupancy(int cls, bool rows, int threads, size_t smem)
 {
     switch (math_mode()) {
-    case MHD_MATH_FAST: return batch_sweep_occupancy_fast(rows, threads, smem);
-    case MHD_MATH_FP64P: return batch_sweep_occupancy_p64(rows, threads, smem);
-    default: return batch_sweep_occupancy_faithful(rows, threads, smem);
+    case MHD_MATH_FAST: return batch_class_occupancy_fast(cls, rows, threads, smem);
+    case MHD_MATH_FP64P: return batch_class_occupancy_p64(cls, rows, threads, smem);
+    default: return batch_class_occupancy_faithful(cls, rows, threads, smem);
     }
 }
 
-// dynamic shared memory of a sweep along axis with `threads` per CTA: the
-// largest tile of any box
-size_t sweep_smem(const mhdgpu_batch &bt, int axis, int threads)
+cudaError_t launch_group(const ClassWork &w, int cls, bool rows, int grid, int threads, size_t smem,
+                         cudaStream_t s)
 {
-    long long fl = 0;
-    const bool rows = axis != 0;
-    for (const BoxDesc &d : bt.box) {
-        const Frame f = make_view(axis, d.nx, d.ny, d.nz);
-        const int tpp = batch_tpp(f.n);
-        const int ppc = std::max(1, threads / tpp);
-        fl = std::max(fl, fx_smem_floats(f.n, ppc, tpp / 32, rows));
-        fl = std::max(fl, ax_smem_floats(f.n, ppc, rows));
+    switch (math_mode()) {
+    case MHD_MATH_FAST: return launch_batch_class_fast(w, cls, rows, grid, threads, smem, s);
+    case MHD_MATH_FP64P: return launch_batch_class_p64(w, cls, rows, grid, threads, smem, s);
+    default: return launch_batch_class_faithful(w, cls, rows, grid, threads, smem, s);
     }
-    return sizeof(float) * (size_t)fl;
 }
 
-// (re)builds the work tables of the sweeps and the grid sizes; synchronous
-int build_tables(mhdgpu_batch &bt)
+// Groups the boxes of every sweep by team class and lays out the per-group
+// tables; sizes only (no device work).  Counter words are reset every step by
+// the clock kernel, so their layout may change between steps.
+void plan_groups(mhdgpu_batch &bt)
 {
-    const int nb = bt.nbox;
-    std::vector<long long> start(6 * (size_t)(3 * nb + 1));
-    std::vector<int> group(6 * (size_t)(3 * nb));
+    bt.groups.clear();
+    size_t off_args = 0, off_start = 0, off_group = 0, off_ctr = 0;
     for (int s = 0; s < 6; ++s) {
+        bt.gbegin[s] = (int)bt.groups.size();
         const int axis = kSweepAxis[s];
-        const bool rows = axis != 0;
-        const int threads = bt.threads[axis];
-        long long *st = &start[(size_t)s * (3 * nb + 1)];
-        long long acc = 0;
-        for (int slot = 0; slot < 3; ++slot) {
-            const int ph = batch_phase(slot, kSweepFluidFirst[s]);
-            for (int i = 0; i < nb; ++i) {
+        for (int cls = 0; cls < kBatchClasses; ++cls) {
+            std::vector<int> members;
+            for (int i = 0; i < bt.nbox; ++i) {
                 const BoxDesc &d = bt.box[i];
-                const Frame f = make_view(axis, d.nx, d.ny, d.nz);
-                const int ppc = threads / batch_tpp(f.n);
-                if (ppc < 1)
-                    return bfail(MHD_ERR_ARG, "mhdgpu_batch: fewer threads per CTA than a pencil's team "
-                                              "(64 for pencils of 65-127 cells, 128 above 128)");
-                st[slot * nb + i] = acc;
-                int g;
-                long long items;
-                if (ph == kPhaseB1) {
-                    g = kB1ItemCells;
-                    items = batch_chunks(f.npen * f.n, g);
-                } else {
-                    const long long tiles = batch_tiles(f, ppc, rows);
-                    g = std::max(1, kItemCells / (ppc * f.n));
-                    items = (tiles + g - 1) / g;
+                if (batch_class(make_view(axis, d.nx, d.ny, d.nz).n) == cls) members.push_back(i);
+            }
+            // a launch carries at most kGroupBoxes boxes' arguments
+            for (size_t m0 = 0; m0 < members.size(); m0 += kGroupBoxes) {
+                BatchGroup g;
+                g.sweep = s;
+                g.cls = cls;
+                const size_t m1 = std::min(members.size(), m0 + (size_t)kGroupBoxes);
+                for (size_t m = m0; m < m1; ++m) {
+                    const BoxDesc &d = bt.box[members[m]];
+                    const Frame f = make_view(axis, d.nx, d.ny, d.nz);
+                    g.boxes.push_back(members[m]);
+                    g.cells += f.npen * f.n;
                 }
-                group[(size_t)s * 3 * nb + slot * nb + i] = g;
-                acc += items;
+                g.nb = (int)g.boxes.size();
+                g.off_args = off_args;
+                g.off_start = off_start;
+                g.off_group = off_group;
+                g.off_ctr = off_ctr;
+                off_args += g.nb;
+                off_start += 3 * g.nb + 1;
+                off_group += 3 * g.nb;
+                off_ctr += 1 + 3 * g.nb;
+                bt.groups.push_back(g);
             }
         }
-        st[3 * nb] = acc;
-        bt.total[s] = acc;
-        if (acc >= (1LL << 31)) return bfail(MHD_ERR_ARG, "mhdgpu_batch: too many work items");
     }
-    for (int axis = 0; axis < 3; ++axis) {
-        bt.smem[axis] = sweep_smem(bt, axis, bt.threads[axis]);
-        if (bt.smem[axis] > 227 * 1024) return bfail(MHD_ERR_ARG, "mhdgpu_batch: tile exceeds shared memory");
-        const int occ = occupancy(axis != 0, bt.threads[axis], bt.smem[axis]);
-        if (occ < 1) return bfail(MHD_ERR_CUDA, "mhdgpu_batch: the sweep kernel cannot be resident");
-        const int cps = std::min(bt.cps[axis], occ);
-        for (int s = 0; s < 6; ++s)
-            if (kSweepAxis[s] == axis)
-                bt.grid[s] = (int)std::max(1LL, std::min((long long)bt.num_sms * cps, bt.total[s]));
+    bt.gbegin[6] = (int)bt.groups.size();
+    bt.nctr = (int)off_ctr;
+}
+
+// (re)builds the work tables and the launch shapes for the current schedule;
+// synchronous
+int build_tables(mhdgpu_batch &bt)
+{
+    std::vector<FluidxArgs> &fa = bt.fa;
+    std::vector<AdvectArgs> &aa = bt.aa;
+    fa.clear();
+    aa.clear();
+    std::vector<long long> start;
+    std::vector<int> group;
+    for (BatchGroup &g : bt.groups) {
+        const int axis = kSweepAxis[g.sweep];
+        const bool rows = axis != 0;
+        const int threads = bt.threads[axis];
+        const int tpp = batch_class_tpp(g.cls);
+        const int ppc = threads / tpp;
+        if (ppc < 1)
+            return bfail(MHD_ERR_ARG, "mhdgpu_batch: fewer threads per CTA than a pencil's team "
+                                      "(64 for pencils of 65-127 cells other than 96, 128 above 128)");
+        std::vector<long long> st(3 * g.nb + 1);
+        std::vector<int> gr(3 * g.nb);
+        long long acc = 0;
+        long long sm = 0;
+        for (int slot = 0; slot < 3; ++slot) {
+            const int ph = batch_phase(slot, kSweepFluidFirst[g.sweep]);
+            for (int b = 0; b < g.nb; ++b) {
+                const BoxDesc &d = bt.box[g.boxes[b]];
+                const Frame f = make_view(axis, d.nx, d.ny, d.nz);
+                int per;
+                long long items;
+                if (ph == kPhaseB1) {
+                    per = kB1ItemCells;
+                    items = batch_chunks(f.npen * f.n, per);
+                } else {
+                    per = std::max(1, kItemCells / (ppc * f.n));
+                    items = (batch_tiles(f, ppc, rows) + per - 1) / per;
+                }
+                st[slot * g.nb + b] = acc;
+                gr[slot * g.nb + b] = per;
+                acc += items;
+                if (slot == 0) {
+                    sm = std::max(sm, fx_smem_floats(f.n, ppc, tpp / 32, rows));
+                    sm = std::max(sm, ax_smem_floats(f.n, ppc, rows));
+                }
+            }
+        }
+        st[3 * g.nb] = acc;
+        if (acc >= (1LL << 31)) return bfail(MHD_ERR_ARG, "mhdgpu_batch: too many work items");
+        g.items = acc;
+        g.smem = sizeof(float) * (size_t)sm;
+        if (g.smem > 227 * 1024) return bfail(MHD_ERR_ARG, "mhdgpu_batch: tile exceeds shared memory");
+        start.insert(start.end(), st.begin(), st.end());
+        group.insert(group.end(), gr.begin(), gr.end());
+        for (int b = 0; b < g.nb; ++b) {
+            const BoxDesc &d = bt.box[g.boxes[b]];
+            const Frame f = make_view(axis, d.nx, d.ny, d.nz);
+            fa.push_back(FluidxArgs{d.u, d.u, d.b, &d.clk->dt, &d.clk->health, f});
+            aa.push_back(AdvectArgs{d.b, d.u, &d.clk->dt, d.scr, d.scr + f.npen * f.n, f});
+        }
+    }
+    // grids: every group gets the whole GPU at its kernel's occupancy (capped
+    // by the schedule).  The groups of a sweep are launched concurrently, so a
+    // group's CTAs take the SMs that the previous group's tail frees; grids
+    // sized to a share of the SMs were measured slower (the groups do not run
+    // side by side, each then runs on its share alone).
+    for (int s = 0; s < 6; ++s) {
+        const int axis = kSweepAxis[s];
+        for (int gi = bt.gbegin[s]; gi < bt.gbegin[s + 1]; ++gi) {
+            BatchGroup &g = bt.groups[gi];
+            const int occ = occupancy(g.cls, axis != 0, bt.threads[axis], g.smem);
+            if (occ < 1) return bfail(MHD_ERR_CUDA, "mhdgpu_batch: a class kernel cannot be resident");
+            g.grid = (int)std::max(1LL, std::min((long long)bt.num_sms * std::min(bt.cps[axis], occ), g.items));
+        }
     }
     BCU(cudaMemcpy(bt.d_start, start.data(), start.size() * sizeof(long long), cudaMemcpyHostToDevice),
         "mhdgpu_batch tables");
@@ -228,27 +313,37 @@ int launch_step(mhdgpu_batch &bt, cudaStream_t s, cudaEvent_t *ev /* 7 events or
         batch_clock_kernel<<<gc, 256, 0, s>>>(bt.d_box, bt.d_tf, nb, bt.cfl_number, bt.d_ctr, bt.nctr);
         BCU(cudaGetLastError(), "mhdgpu_batch_advance clock");
     }
-    const int math = math_mode();
     for (int sw = 0; sw < 6; ++sw) {
         const int axis = kSweepAxis[sw];
-        SweepWork w;
-        w.box = bt.d_box;
-        w.start = bt.d_start + (size_t)sw * (3 * nb + 1);
-        w.group = bt.d_group + (size_t)sw * 3 * nb;
-        w.claim = bt.d_ctr + sw;
-        w.done = bt.d_ctr + 6 + (size_t)sw * 3 * nb;
-        w.abort = bt.d_abort;
-        w.nbox = nb;
-        w.axis = axis;
-        w.fluid_first = kSweepFluidFirst[sw];
+        const int g0 = bt.gbegin[sw], g1 = bt.gbegin[sw + 1];
         if (ev) BCU(cudaEventRecord(ev[sw], s), "mhdgpu_batch event");
-        ProfScope ps(MHD_KCLASS_BATCH, 1, s);
-        const bool rows = axis != 0;
-        const cudaError_t e =
-            math == MHD_MATH_FAST    ? launch_batch_sweep_fast(w, rows, bt.grid[sw], bt.threads[axis], bt.smem[axis], s)
-            : math == MHD_MATH_FP64P ? launch_batch_sweep_p64(w, rows, bt.grid[sw], bt.threads[axis], bt.smem[axis], s)
-                                     : launch_batch_sweep_faithful(w, rows, bt.grid[sw], bt.threads[axis], bt.smem[axis], s);
-        BCU(e, "mhdgpu_batch_advance sweep");
+        ProfScope ps(MHD_KCLASS_BATCH, g1 - g0, s);
+        const bool fan = g1 - g0 > 1;
+        if (fan) BCU(cudaEventRecord(bt.fork, s), "mhdgpu_batch fork");
+        for (int gi = g0; gi < g1; ++gi) {
+            const BatchGroup &g = bt.groups[gi];
+            ClassWork &w = bt.work;
+            std::copy(bt.fa.begin() + g.off_args, bt.fa.begin() + g.off_args + g.nb, w.fa);
+            std::copy(bt.aa.begin() + g.off_args, bt.aa.begin() + g.off_args + g.nb, w.aa);
+            w.start = bt.d_start + g.off_start;
+            w.group = bt.d_group + g.off_group;
+            w.claim = bt.d_ctr + g.off_ctr;
+            w.done = bt.d_ctr + g.off_ctr + 1;
+            w.abort = bt.d_abort;
+            w.nb = g.nb;
+            w.fluid_first = kSweepFluidFirst[sw];
+            w.stall_extra = gi == 0 ? bt.stall_extra : 0u;
+            cudaStream_t gs = s;
+            if (fan) {
+                gs = bt.side[(gi - g0) % kBatchClasses];
+                BCU(cudaStreamWaitEvent(gs, bt.fork, 0), "mhdgpu_batch fork");
+            }
+            BCU(launch_group(w, g.cls, axis != 0, g.grid, bt.threads[axis], g.smem, gs), "mhdgpu_batch_advance sweep");
+            if (fan) {
+                BCU(cudaEventRecord(bt.join[(gi - g0) % kBatchClasses], gs), "mhdgpu_batch join");
+                BCU(cudaStreamWaitEvent(s, bt.join[(gi - g0) % kBatchClasses], 0), "mhdgpu_batch join");
+            }
+        }
     }
     if (ev) BCU(cudaEventRecord(ev[6], s), "mhdgpu_batch event");
     return MHD_OK;
@@ -263,10 +358,12 @@ size_t mhdgpu_batch_workspace_bytes(int nbox, const int *dims)
     if (!dims_ok(nbox, dims)) return 0;
     long long cells = 0;
     for (int i = 0; i < nbox; ++i) cells += cells_of(dims + 3 * i);
-    const size_t nctr = 6 + 18 * (size_t)nbox + 1;
+    // upper bounds of the tables: 6 sweeps x (8 classes + a split per 64 boxes)
+    const size_t ngroups = 6 * (8 + (size_t)nbox / kGroupBoxes + 1);
+    const size_t nctr = ngroups + 18 * (size_t)nbox + 1;
     return sizeof(float) * 2 * (size_t)cells + nbox * (sizeof(BoxDesc) + sizeof(mhdgpu_clock) + sizeof(float)) +
-           nctr * sizeof(unsigned) + (6 * (3 * (size_t)nbox + 1) + nbox + 1) * sizeof(long long) +
-           18 * (size_t)nbox * sizeof(int);
+           nctr * sizeof(unsigned) +
+           (18 * (size_t)nbox + ngroups + nbox + 1) * sizeof(long long) + 18 * (size_t)nbox * sizeof(int);
 }
 
 int mhdgpu_batch_create(mhdgpu_batch **out, int nbox, const int *dims, float *const *d_u,
@@ -297,22 +394,12 @@ int mhdgpu_batch_create(mhdgpu_batch **out, int nbox, const int *dims, float *co
         cells += nc;
     }
     cfl_start[nbox] = bt->cfl_total;
-    bt->nctr = 6 + 18 * nbox;
     std::vector<float> htf(nbox, 0.0f);
     if (tf) std::copy(tf, tf + nbox, htf.begin());
     if (e == cudaSuccess) e = cudaMalloc(&bt->d_box, nbox * sizeof(BoxDesc));
     if (e == cudaSuccess) e = cudaMalloc(&bt->d_clk, nbox * sizeof(mhdgpu_clock));
     if (e == cudaSuccess) e = cudaMalloc(&bt->d_scr, 2 * sizeof(float) * (size_t)cells);
     if (e == cudaSuccess) e = cudaMalloc(&bt->d_tf, nbox * sizeof(float));
-    if (e == cudaSuccess) e = cudaMalloc(&bt->d_ctr, (bt->nctr + 1) * sizeof(unsigned));
-    if (e == cudaSuccess) e = cudaMalloc(&bt->d_start, 6 * (3 * (size_t)nbox + 1) * sizeof(long long));
-    if (e == cudaSuccess) e = cudaMalloc(&bt->d_group, 6 * 3 * (size_t)nbox * sizeof(int));
-    if (e == cudaSuccess) e = cudaMalloc(&bt->d_cfl_start, (nbox + 1) * sizeof(long long));
-    if (e != cudaSuccess) {
-        delete bt;
-        return bcuda(e, "mhdgpu_batch_create");
-    }
-    bt->d_abort = bt->d_ctr + bt->nctr;
     bt->box.resize(nbox);
     long long off = 0;
     for (int i = 0; i < nbox; ++i) {
@@ -327,6 +414,22 @@ int mhdgpu_batch_create(mhdgpu_batch **out, int nbox, const int *dims, float *co
         d.pad = 0;
         off += cells_of(dims + 3 * i);
     }
+    plan_groups(*bt);
+    const size_t ngroups = bt->groups.size();
+    if (e == cudaSuccess) e = cudaMalloc(&bt->d_ctr, (bt->nctr + 1) * sizeof(unsigned));
+    if (e == cudaSuccess) e = cudaMalloc(&bt->d_start, (18 * (size_t)nbox + ngroups) * sizeof(long long));
+    if (e == cudaSuccess) e = cudaMalloc(&bt->d_group, 18 * (size_t)nbox * sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&bt->d_cfl_start, (nbox + 1) * sizeof(long long));
+    for (int i = 0; i < kBatchClasses && e == cudaSuccess; ++i) {
+        e = cudaStreamCreateWithFlags(&bt->side[i], cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&bt->join[i], cudaEventDisableTiming);
+    }
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&bt->fork, cudaEventDisableTiming);
+    if (e != cudaSuccess) {
+        delete bt;
+        return bcuda(e, "mhdgpu_batch_create");
+    }
+    bt->d_abort = bt->d_ctr + bt->nctr;
     e = cudaMemcpy(bt->d_box, bt->box.data(), nbox * sizeof(BoxDesc), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemset(bt->d_clk, 0, nbox * sizeof(mhdgpu_clock));
     if (e == cudaSuccess) e = cudaMemset(bt->d_ctr, 0, (bt->nctr + 1) * sizeof(unsigned));
@@ -409,6 +512,13 @@ int mhdgpu_batch_get_schedule(const mhdgpu_batch *bt, int axis, int *threads, in
     return MHD_OK;
 }
 
+int mhdgpu_batch_inject_stall(mhdgpu_batch *bt)
+{
+    if (!bt) return bfail(MHD_ERR_ARG, "mhdgpu_batch_inject_stall: null handle");
+    bt->stall_extra = 1;
+    return MHD_OK;
+}
+
 int mhdgpu_batch_tune(mhdgpu_batch *bt, mhdgpu_stream_t stream)
 {
     if (!bt) return bfail(MHD_ERR_ARG, "mhdgpu_batch_tune: null handle");
@@ -445,7 +555,8 @@ int mhdgpu_batch_tune(mhdgpu_batch *bt, mhdgpu_stream_t stream)
     float best[3] = {1e30f, 1e30f, 1e30f};
     int best_t[3] = {keep_t[0], keep_t[1], keep_t[2]}, best_c[3] = {keep_c[0], keep_c[1], keep_c[2]};
     for (int ti = 0; ti < 3 && st == MHD_OK; ++ti) {
-        for (int cps = 1; cps <= 4 && st == MHD_OK; ++cps) {
+        for (int cps : {2, 4, 8}) {
+            if (st != MHD_OK) break;
             for (int a = 0; a < 3; ++a) {
                 bt->threads[a] = kThreadChoices[ti];
                 bt->cps[a] = cps;

@@ -1,20 +1,17 @@
-// batch_faithful.cu - the batched sweep kernels under the faithful math
-// policy (batch_kernel.cuh).
+// batch_faithful.cu - the batched class kernels under the faithful policy (batch_kernel.cuh).
 #include "batch_kernel.cuh"
 
 namespace mhd {
 
-cudaError_t launch_batch_sweep_faithful(const SweepWork &w, bool rows, int grid, int threads, size_t smem,
-                                        cudaStream_t s)
+cudaError_t launch_batch_class_faithful(const ClassWork &w, int cls, bool rows, int grid, int threads,
+                                  size_t smem, cudaStream_t s)
 {
-    return rows ? launch_batch_sweep_inst<Faithful, true>(w, grid, threads, smem, s)
-                : launch_batch_sweep_inst<Faithful, false>(w, grid, threads, smem, s);
+    return launch_batch_class_policy<Faithful>(w, cls, rows, grid, threads, smem, s);
 }
 
-int batch_sweep_occupancy_faithful(bool rows, int threads, size_t smem)
+int batch_class_occupancy_faithful(int cls, bool rows, int threads, size_t smem)
 {
-    return rows ? batch_sweep_occupancy_inst<Faithful, true>(threads, smem)
-                : batch_sweep_occupancy_inst<Faithful, false>(threads, smem);
+    return batch_class_occupancy_policy<Faithful>(cls, rows, threads, smem);
 }
 
 }  // namespace mhd

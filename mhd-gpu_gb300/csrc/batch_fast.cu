@@ -1,20 +1,17 @@
-// batch_fast.cu - the batched sweep kernels under the fast math
-// policy (batch_kernel.cuh).
+// batch_fast.cu - the batched class kernels under the fast policy (batch_kernel.cuh).
 #include "batch_kernel.cuh"
 
 namespace mhd {
 
-cudaError_t launch_batch_sweep_fast(const SweepWork &w, bool rows, int grid, int threads, size_t smem,
-                                        cudaStream_t s)
+cudaError_t launch_batch_class_fast(const ClassWork &w, int cls, bool rows, int grid, int threads,
+                                  size_t smem, cudaStream_t s)
 {
-    return rows ? launch_batch_sweep_inst<Fast, true>(w, grid, threads, smem, s)
-                : launch_batch_sweep_inst<Fast, false>(w, grid, threads, smem, s);
+    return launch_batch_class_policy<Fast>(w, cls, rows, grid, threads, smem, s);
 }
 
-int batch_sweep_occupancy_fast(bool rows, int threads, size_t smem)
+int batch_class_occupancy_fast(int cls, bool rows, int threads, size_t smem)
 {
-    return rows ? batch_sweep_occupancy_inst<Fast, true>(threads, smem)
-                : batch_sweep_occupancy_inst<Fast, false>(threads, smem);
+    return batch_class_occupancy_policy<Fast>(cls, rows, threads, smem);
 }
 
 }  // namespace mhd

@@ -1,33 +1,33 @@
 // batch_kernel.cuh - the batched ensemble: many independent periodic boxes of
-// uneven, non-cubic sizes advance together, one persistent launch per sweep.
+// uneven, non-cubic sizes advance together, each sweep one set of concurrent
+// persistent launches.
 //
 // There is no counterpart in the reference (its drivers advance one box,
 // Heterogeneous_MHD/C/mhd.c:59-125); each box follows exactly the fused
 // transpose-free step of one box (the same tile functions, the same rounding),
 // so a box advanced in a batch is bit-identical to the box advanced alone.
 //
-// Work list.  A sweep (x, y, z, z, y, x) has three phases per box: fluid
-// tiles (fluidx_tile), field tiles (advect_tile) and b(1) chunks
-// (advect_b1_cell), in the order fluid, field, b(1) on the way out and field,
-// b(1), fluid on the way back (mhd.c:72-119).  The launch's items are the
-// (slot, box, tile) triples, numbered slot-major through a prefix table, and
-// CTAs claim them in that order from one atomic counter.  A phase of a box
-// needs the box's previous phase complete (the field update reads u at the
-// j-1 and k-1 pencils; b(1) reads the fluxes of the j+1 and k+1 pencils); a
-// CTA that claims such an item waits on the box's completion counter of the
-// previous slot.  Every item waited on was claimed earlier by a running CTA,
-// and the earliest unfinished item never waits, so the launch always drains
-// whatever the residency; the wait is bounded all the same (batch_wait).
+// Team classes.  A sweep's boxes are grouped by the team class of their pencil
+// length along the sweep (the length is a compile-time constant for 32, 48,
+// 64, 96 and 128 cells), and each group is one persistent launch of a kernel
+// specialised for its class; the groups of a sweep run concurrently (parallel
+// branches of the step's graph) and the next sweep starts when all are done.
+// A kernel holds one class only because classes compiled into one kernel share
+// its register allocation and spill registers that none of them needs alone.
 //
-// Team classes.  One kernel serves every pencil length of a sweep: the team
-// shape is picked per item from the box's pencil length, with the length a
-// compile-time constant for the ensemble's sizes (32, 48, 64, 96, 128) and at
-// most three cells per thread.  Each class's tile is a separate (not inlined)
-// function: inlined together in one kernel the classes spill registers that
-// each of them alone does not need, and the call costs once per tile.  The
-// kernel runs at 80 registers (3 CTAs of 256 threads per SM), where the
-// full-team classes do not spill.  The item arguments are staged in shared
-// memory.
+// Work list of a group.  A sweep has three phases per box: fluid tiles
+// (fluidx_tile), field tiles (advect_tile) and b(1) chunks (advect_b1_cell),
+// in the order fluid, field, b(1) on the way out and field, b(1), fluid on the
+// way back (mhd.c:72-119).  The launch's items are (slot, box, item) triples,
+// numbered slot-major through a prefix table, and CTAs claim them in that order
+// from one atomic counter (the next claim is issued while the current item
+// runs).  A phase of a box needs the box's previous phase complete (the field
+// update reads u at the j-1 and k-1 pencils; b(1) reads the fluxes of the j+1
+// and k+1 pencils); a CTA that claims such an item waits on the box's
+// completion counter of the previous slot.  Every item waited on was claimed
+// earlier by a running CTA, and the earliest unfinished item never waits, so
+// the launch always drains whatever the residency; the wait is bounded all the
+// same (batch_wait).
 #pragma once
 
 #include "advect_kernel.cuh"
@@ -37,6 +37,7 @@
 namespace mhd {
 
 constexpr int kBatchMaxPencil = MHD_BATCH_MAX_PENCIL;
+constexpr int kBatchClasses = 8;
 
 struct BoxDesc {
     float *u, *b;          // the caller's state, reference layout
@@ -45,10 +46,9 @@ struct BoxDesc {
     int nx, ny, nz, pad;
 };
 
-// team class by pencil length (1 <= n <= kBatchMaxPencil); the length is a
-// compile-time constant for 32, 48, 64, 96 and 128 cells:
+// team class by pencil length (1 <= n <= kBatchMaxPencil):
 //   0: 32 = 1 x 32 threads     1: 64 = 2 x 32      2: 96 = 3 x 32
-//   3: 128 = 2 x 64            4: 48 (2 x 32, 16 slots idle)
+//   3: 128 = 4 x 32            4: 48 (2 x 32, 16 slots idle)
 //   5: other n < 64 (2 x 32)   6: other n < 128 (2 x 64)   7: n <= 256 (2 x 128)
 __host__ __device__ inline int batch_class(int n)
 {
@@ -61,12 +61,9 @@ __host__ __device__ inline int batch_class(int n)
     default: return n < 64 ? 5 : (n < 128 ? 6 : 7);
     }
 }
-// threads per pencil of the class
-__host__ __device__ inline int batch_tpp(int n)
-{
-    const int c = batch_class(n);
-    return (c == 3 || c == 6) ? 64 : (c == 7 ? 128 : 32);
-}
+// threads per pencil of a class
+__host__ __device__ inline int batch_class_tpp(int c) { return c == 6 ? 64 : (c == 7 ? 128 : 32); }
+__host__ __device__ inline int batch_tpp(int n) { return batch_class_tpp(batch_class(n)); }
 
 // items of a phase: tiles of ppc pencils (contiguous pencils are numbered
 // linearly, pencils across memory by (j-block, k)), or chunks of cells
@@ -85,14 +82,22 @@ __host__ __device__ inline int batch_phase(int slot, int fluid_first)
     return fluid_first ? slot : (slot + 1) % 3;
 }
 
-struct SweepWork {
-    const BoxDesc *box;
-    const long long *start;   // 3*nbox + 1 prefix sums of item counts, entry slot*nbox + box
-    const int *group;         // 3*nbox: tiles per item (fluid, field) or cells per item (b(1))
+// one persistent launch: up to kGroupBoxes boxes of one class in one sweep.
+// The boxes' arguments travel in the launch's parameter block (read through
+// the constant cache, like a single-box kernel's arguments), not in global
+// memory, so the tile code reloads them for free instead of holding them in
+// registers.
+constexpr int kGroupBoxes = 64;
+struct ClassWork {
+    FluidxArgs fa[kGroupBoxes];   // each box's fluid-sweep arguments (frame of the sweep)
+    AdvectArgs aa[kGroupBoxes];   // field-sweep arguments
+    const long long *start;   // 3*nb + 1 prefix sums of item counts, entry slot*nb + box
+    const int *group;         // 3*nb: tiles per item (fluid, field) or cells per item (b(1))
     unsigned *claim;          // next item of this launch (zeroed by the clock kernel)
-    unsigned *done;           // 3*nbox items finished per (slot, box) (zeroed likewise)
+    unsigned *done;           // 3*nb items finished per (slot, box) (zeroed likewise)
     unsigned *abort;          // nonzero once a dependency wait gave up
-    int nbox, axis, fluid_first;
+    int nb, fluid_first;
+    unsigned stall_extra;     // test hook: extra items box 0's second phase waits for
 };
 
 // an item covers about this many cells (several tiles of small pencils), so
@@ -141,48 +146,6 @@ __device__ inline bool batch_wait(const unsigned *ctr, unsigned target, unsigned
     return false;
 }
 
-template <int C, int W, class M, bool ROWS, int NT>
-__device__ __noinline__ void batch_fluidx_class(const FluidxArgs &a, long long tile)
-{
-    fluidx_tile<C, W, M, ROWS, NT>(a, tile);
-}
-
-template <int C, int W, class M, bool ROWS, int NT>
-__device__ __noinline__ void batch_advect_class(const AdvectArgs &a, long long tile)
-{
-    advect_tile<C, W, M, ROWS, NT>(a, tile);
-}
-
-template <class M, bool ROWS>
-__device__ __forceinline__ void batch_fluidx(const FluidxArgs &a, long long tile)
-{
-    switch (batch_class(a.f.n)) {
-    case 0: batch_fluidx_class<1, 1, M, ROWS, 32>(a, tile); break;
-    case 1: batch_fluidx_class<2, 1, M, ROWS, 64>(a, tile); break;
-    case 2: batch_fluidx_class<3, 1, M, ROWS, 96>(a, tile); break;
-    case 3: batch_fluidx_class<2, 2, M, ROWS, 128>(a, tile); break;
-    case 4: batch_fluidx_class<2, 1, M, ROWS, 48>(a, tile); break;
-    case 5: batch_fluidx_class<2, 1, M, ROWS, 0>(a, tile); break;
-    case 6: batch_fluidx_class<2, 2, M, ROWS, 0>(a, tile); break;
-    default: batch_fluidx_class<2, 4, M, ROWS, 0>(a, tile); break;
-    }
-}
-
-template <class M, bool ROWS>
-__device__ __forceinline__ void batch_advect(const AdvectArgs &a, long long tile)
-{
-    switch (batch_class(a.f.n)) {
-    case 0: batch_advect_class<1, 1, M, ROWS, 32>(a, tile); break;
-    case 1: batch_advect_class<2, 1, M, ROWS, 64>(a, tile); break;
-    case 2: batch_advect_class<3, 1, M, ROWS, 96>(a, tile); break;
-    case 3: batch_advect_class<2, 2, M, ROWS, 128>(a, tile); break;
-    case 4: batch_advect_class<2, 1, M, ROWS, 48>(a, tile); break;
-    case 5: batch_advect_class<2, 1, M, ROWS, 0>(a, tile); break;
-    case 6: batch_advect_class<2, 2, M, ROWS, 0>(a, tile); break;
-    default: batch_advect_class<2, 4, M, ROWS, 0>(a, tile); break;
-    }
-}
-
 __device__ __forceinline__ void batch_b1(const AdvectArgs &a, long long c0, int cells)
 {
     const long long ncell = a.f.npen * a.f.n;
@@ -190,17 +153,15 @@ __device__ __forceinline__ void batch_b1(const AdvectArgs &a, long long c0, int 
     for (long long c = c0 + threadIdx.x; c < c1; c += blockDim.x) advect_b1_cell(a.b, a.sA, a.sB, a.f, c);
 }
 
-// One sweep of every box.  At most 256 threads (8 pencils of one warp per
-// CTA); 3 CTAs per SM bound the registers at 80.
-template <class M, bool ROWS>
-__global__ void __launch_bounds__(256, 3)
-batch_sweep_kernel(SweepWork w)
+// One sweep of the boxes of one class.  At most 256 threads per CTA; MINB
+// resident CTAs of 256 threads per SM bound the registers (65536 / (256 MINB)).
+template <int CPL, int WPP, class M, bool ROWS, int NT, int MINB>
+__global__ void __launch_bounds__(256, MINB)
+batch_class_kernel(const __grid_constant__ ClassWork w)
 {
     __shared__ int s_e, s_run;
     __shared__ long long s_local;
-    __shared__ FluidxArgs s_fa;
-    __shared__ AdvectArgs s_aa;
-    const long long total = w.start[3 * w.nbox];
+    const long long total = w.start[3 * w.nb];
     // thread 0 claims the next item while the CTA works on the current one
     unsigned it = 0;
     if (threadIdx.x == 0) it = atomicAdd(w.claim, 1u);
@@ -209,7 +170,7 @@ batch_sweep_kernel(SweepWork w)
             int e = -1, run = 0;
             long long local = 0;
             if ((long long)it < total) {
-                int lo = 0, hi = 3 * w.nbox - 1;   // last entry with start <= it
+                int lo = 0, hi = 3 * w.nb - 1;   // last entry with start <= it
                 while (lo < hi) {
                     const int mid = (lo + hi + 1) >> 1;
                     if (w.start[mid] <= (long long)it) lo = mid;
@@ -218,15 +179,12 @@ batch_sweep_kernel(SweepWork w)
                 e = lo;
                 local = (long long)it - w.start[e];
                 run = 1;
-                if (e >= w.nbox) {   // wait for the box's previous phase
-                    const int prev = e - w.nbox;
-                    const unsigned need = (unsigned)(w.start[prev + 1] - w.start[prev]);
-                    run = batch_wait(w.done + prev, need, w.abort, &w.box[e % w.nbox].clk->health);
+                if (e >= w.nb) {   // wait for the box's previous phase
+                    const int prev = e - w.nb;
+                    const unsigned need = (unsigned)(w.start[prev + 1] - w.start[prev]) +
+                                          (prev == 0 ? w.stall_extra : 0u);
+                    run = batch_wait(w.done + prev, need, w.abort, w.fa[e % w.nb].health);
                 }
-                const BoxDesc d = w.box[e % w.nbox];
-                const Frame f = make_view(w.axis, d.nx, d.ny, d.nz);
-                s_fa = FluidxArgs{d.u, d.u, d.b, &d.clk->dt, &d.clk->health, f};
-                s_aa = AdvectArgs{d.b, d.u, &d.clk->dt, d.scr, d.scr + f.npen * f.n, f};
                 it = atomicAdd(w.claim, 1u);
             }
             s_e = e;
@@ -237,19 +195,20 @@ batch_sweep_kernel(SweepWork w)
         const int e = s_e;
         if (e < 0) break;
         if (s_run) {
-            const int ph = batch_phase(e / w.nbox, w.fluid_first);
+            const int slot = e / w.nb, bx = e - slot * w.nb;
+            const int ph = batch_phase(slot, w.fluid_first);
             const long long local = s_local;
             const int g = w.group[e];
             if (ph == kPhaseB1) {
-                batch_b1(s_aa, local * g, g);
+                batch_b1(w.aa[bx], local * g, g);
             } else {
-                const int ppc = blockDim.x / batch_tpp(s_fa.f.n);
+                const int ppc = blockDim.x / (32 * WPP);
                 const long long t0 = local * g;
-                const long long t1 = min(t0 + g, batch_tiles(s_fa.f, ppc, ROWS));
+                const long long t1 = min(t0 + g, batch_tiles(w.fa[bx].f, ppc, ROWS));
                 for (long long t = t0; t < t1; ++t) {
                     if (t > t0) __syncthreads();   // the previous tile's shared memory is consumed
-                    if (ph == kPhaseFluid) batch_fluidx<M, ROWS>(s_fa, t);
-                    else batch_advect<M, ROWS>(s_aa, t);
+                    if (ph == kPhaseFluid) fluidx_tile<CPL, WPP, M, ROWS, NT>(w.fa[bx], t);
+                    else advect_tile<CPL, WPP, M, ROWS, NT>(w.aa[bx], t);
                 }
             }
         }
@@ -259,44 +218,59 @@ batch_sweep_kernel(SweepWork w)
     }
 }
 
-template <class M, bool ROWS>
-cudaError_t launch_batch_sweep_inst(const SweepWork &w, int grid, int threads, size_t smem, cudaStream_t s)
-{
-    static size_t smem_set = 0;
-    if (smem > 227 * 1024) return cudaErrorInvalidConfiguration;
-    if (smem > 48 * 1024 && smem_set < smem) {
-        cudaError_t e = cudaFuncSetAttribute(batch_sweep_kernel<M, ROWS>,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        smem_set = smem;
-    }
-    batch_sweep_kernel<M, ROWS><<<grid, threads, smem, s>>>(w);
-    return cudaGetLastError();
-}
+// the classes: (class, cells per thread, warps per pencil, compile-time
+// length, CTAs per SM the registers are bounded for).  The full-team classes
+// fit 64 registers without spilling; uncapped, the compiler spends up to 128.
+#define MHD_BATCH_CLASSES(X)                                                           \
+    X(0, 1, 1, 32, 4) X(1, 2, 1, 64, 4) X(2, 3, 1, 96, 4) X(3, 4, 1, 128, 4) X(4, 2, 1, 48, 3) \
+    X(5, 2, 1, 0, 2) X(6, 2, 2, 0, 2) X(7, 2, 4, 0, 2)
 
 template <class M, bool ROWS>
-int batch_sweep_occupancy_inst(int threads, size_t smem)
+const void *batch_class_kernel_ptr(int cls)
 {
+    switch (cls) {
+#define MHD_BK(C, CPL, WPP, NT, MINB) \
+    case C: return (const void *)batch_class_kernel<CPL, WPP, M, ROWS, NT, MINB>;
+        MHD_BATCH_CLASSES(MHD_BK)
+#undef MHD_BK
+    default: return nullptr;
+    }
+}
+
+template <class M>
+cudaError_t launch_batch_class_policy(const ClassWork &w, int cls, bool rows, int grid, int threads,
+                                      size_t smem, cudaStream_t s)
+{
+    const void *fn = rows ? batch_class_kernel_ptr<M, true>(cls) : batch_class_kernel_ptr<M, false>(cls);
+    if (!fn || smem > 227 * 1024) return cudaErrorInvalidConfiguration;
+    void *args[] = {const_cast<ClassWork *>(&w)};
+    return cudaLaunchKernel(fn, dim3(grid), dim3(threads), args, smem, s);
+}
+
+// resident CTAs per SM of a class kernel; also raises its dynamic shared
+// memory limit to smem (the launch relies on it)
+template <class M>
+int batch_class_occupancy_policy(int cls, bool rows, int threads, size_t smem)
+{
+    const void *fn = rows ? batch_class_kernel_ptr<M, true>(cls) : batch_class_kernel_ptr<M, false>(cls);
+    if (!fn) return 0;
     if (smem > 48 * 1024 &&
-        cudaFuncSetAttribute(batch_sweep_kernel<M, ROWS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)smem) != cudaSuccess)
+        cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
         return 0;
     int nb = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, batch_sweep_kernel<M, ROWS>, threads, smem) !=
-        cudaSuccess)
-        return 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, threads, smem) != cudaSuccess) return 0;
     return nb;
 }
 
-// per-policy launchers (batch_faithful.cu, batch_fast.cu, batch_p64.cu)
-cudaError_t launch_batch_sweep_faithful(const SweepWork &w, bool rows, int grid, int threads, size_t smem,
-                                        cudaStream_t s);
-cudaError_t launch_batch_sweep_fast(const SweepWork &w, bool rows, int grid, int threads, size_t smem,
-                                    cudaStream_t s);
-int batch_sweep_occupancy_faithful(bool rows, int threads, size_t smem);
-int batch_sweep_occupancy_fast(bool rows, int threads, size_t smem);
-cudaError_t launch_batch_sweep_p64(const SweepWork &w, bool rows, int grid, int threads, size_t smem,
-                                   cudaStream_t s);
-int batch_sweep_occupancy_p64(bool rows, int threads, size_t smem);
+// per-policy entry points (batch_faithful.cu, batch_fast.cu, batch_p64.cu)
+cudaError_t launch_batch_class_faithful(const ClassWork &w, int cls, bool rows, int grid, int threads,
+                                        size_t smem, cudaStream_t s);
+cudaError_t launch_batch_class_fast(const ClassWork &w, int cls, bool rows, int grid, int threads,
+                                    size_t smem, cudaStream_t s);
+cudaError_t launch_batch_class_p64(const ClassWork &w, int cls, bool rows, int grid, int threads,
+                                   size_t smem, cudaStream_t s);
+int batch_class_occupancy_faithful(int cls, bool rows, int threads, size_t smem);
+int batch_class_occupancy_fast(int cls, bool rows, int threads, size_t smem);
+int batch_class_occupancy_p64(int cls, bool rows, int threads, size_t smem);
 
 }  // namespace mhd

@@ -1,20 +1,18 @@
-// batch_p64.cu - the batched sweep kernels under the faithful policy
-// with FP64 pressure recovery in low-beta cells (batch_kernel.cuh).
+// batch_p64.cu - the batched class kernels under the faithful policy with
+// FP64 pressure recovery in low-beta cells (batch_kernel.cuh).
 #include "batch_kernel.cuh"
 
 namespace mhd {
 
-cudaError_t launch_batch_sweep_p64(const SweepWork &w, bool rows, int grid, int threads, size_t smem,
-                                        cudaStream_t s)
+cudaError_t launch_batch_class_p64(const ClassWork &w, int cls, bool rows, int grid, int threads,
+                                  size_t smem, cudaStream_t s)
 {
-    return rows ? launch_batch_sweep_inst<Recover64, true>(w, grid, threads, smem, s)
-                : launch_batch_sweep_inst<Recover64, false>(w, grid, threads, smem, s);
+    return launch_batch_class_policy<Recover64>(w, cls, rows, grid, threads, smem, s);
 }
 
-int batch_sweep_occupancy_p64(bool rows, int threads, size_t smem)
+int batch_class_occupancy_p64(int cls, bool rows, int threads, size_t smem)
 {
-    return rows ? batch_sweep_occupancy_inst<Recover64, true>(threads, smem)
-                : batch_sweep_occupancy_inst<Recover64, false>(threads, smem);
+    return batch_class_occupancy_policy<Recover64>(cls, rows, threads, smem);
 }
 
 }  // namespace mhd

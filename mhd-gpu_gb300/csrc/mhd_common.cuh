@@ -151,17 +151,20 @@ __device__ __forceinline__ void flag_health(unsigned *health, unsigned bits)
 
 // Asynchronous 4-byte global -> shared copy (cp.async, no register round
 // trip): a thread can have all of its staging copies in flight at once.
-// Complete them with cp_async_wait_all() and then a barrier.
+// Complete them with cp_async_wait_all() and then a barrier.  The issue
+// carries no compiler memory clobber, so the staging loops keep their
+// addresses in registers; the wait has one, and nothing touches a
+// destination before its wait.
 __device__ __forceinline__ void cp_async4(float *smem_dst, const float *gmem_src)
 {
     const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem_dst));
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem_src) : "memory");
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem_src));
 }
 
 __device__ __forceinline__ void cp_async16(void *smem_dst, const void *gmem_src)
 {
     const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem_dst));
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem_src) : "memory");
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem_src));
 }
 
 __device__ __forceinline__ void cp_async_wait_all()

@@ -43,7 +43,7 @@ EXPORTS = [
     "mhdgpu_read_state", "mhdgpu_write_state", "mhdgpu_write_result", "mhdgpu_write_check",
     "mhdgpu_batch_workspace_bytes", "mhdgpu_batch_create", "mhdgpu_batch_destroy",
     "mhdgpu_batch_advance", "mhdgpu_batch_read_clocks", "mhdgpu_batch_set_schedule",
-    "mhdgpu_batch_get_schedule", "mhdgpu_batch_tune",
+    "mhdgpu_batch_get_schedule", "mhdgpu_batch_tune", "mhdgpu_batch_inject_stall",
     # include/mhdgpu_compat.h
     "fluidx", "advectbyzx", "transpose12", "transpose13", "calcfl", "copy_matrix",
     "mhdgpu_compat_status",
@@ -117,6 +117,7 @@ def lib() -> C.CDLL:
             "mhdgpu_batch_set_schedule": (I, [P, I, I, I]),
             "mhdgpu_batch_get_schedule": (I, [P, I, P, P]),
             "mhdgpu_batch_tune": (I, [P, P]),
+            "mhdgpu_batch_inject_stall": (I, [P]),
             "calcfl": (F, [P, P, P, P, P]),
             "cfl_": (F, [P, P, P, P, P]),
             "mhdgpu_compat_status": (I, []),
@@ -415,6 +416,10 @@ class Batch:
         """Autotune the block schedule per axis; returns [(threads, ctas_per_sm)] * 3."""
         _check(lib().mhdgpu_batch_tune(self.h, _stream(stream)))
         return [self.get_schedule(a) for a in range(3)]
+
+    def inject_stall(self):
+        """Failure-path test hook (mhdgpu_batch_inject_stall)."""
+        _check(lib().mhdgpu_batch_inject_stall(self.h))
 
     def close(self):
         if self.h:

@@ -129,7 +129,7 @@ def test_batch_tune_restores_state(gpu):
     boxes = [(dev(u), dev(b), d) for (u, b), d in zip(states, dims)]
     bt = gpu.Batch(boxes, cfl_number=0.7)
     sched = bt.tune()
-    assert all(t in (64, 128, 256) and 1 <= c <= 4 for t, c in sched)
+    assert all(t in (64, 128, 256) and c in (2, 4, 8) for t, c in sched)
     for (u, b, _), (u0, b0) in zip(boxes, states):
         assert bits_equal(host(u), u0) and bits_equal(host(b), b0)
     assert all(c.iter == 0 and c.t == 0.0 for c in bt.clocks())
@@ -220,3 +220,30 @@ def test_batch_ensemble_workload_sample(gpu):
         # round-off of the face updates: a few ulps of |B| per step
         bound = 2 * ics.div_b(e["b"], *e["dims"]) + 5 * 16 * 2.0 ** -24 * float(np.abs(b).max())
         assert ics.div_b(b, *e["dims"]) < bound
+
+
+def test_batch_wait_timeout_is_reported_and_context_survives(gpu):
+    """A dependency wait that cannot be satisfied (the test hook asks for one
+    item more than exist) gives up after its bounded limit: the box's health
+    carries MHD_HEALTH_STALL, the launch drains, the host reads
+    MHD_ERR_TIMEOUT, and the CUDA context keeps working for a new batch."""
+    import time
+    import torch
+    dims = [(16, 8, 8), (8, 16, 8)]
+    states = _states(dims, seed=6)
+    boxes = [(dev(u), dev(b), d) for (u, b), d in zip(states, dims)]
+    bt = gpu.Batch(boxes, cfl_number=0.7)
+    bt.inject_stall()
+    t0 = time.time()
+    bt.advance(1)
+    torch.cuda.synchronize()
+    el = time.time() - t0
+    with pytest.raises(gpu.MhdError) as ei:
+        bt.clocks()
+    assert ei.value.status == gpu.MHD_ERR_TIMEOUT
+    assert bt.clocks(check=False)[0].health & gpu.MHD_HEALTH_STALL
+    assert 1.0 < el < 30.0
+    bt.close()
+    ref = _per_box(gpu, states, dims, 2, 0.7)
+    got = _batched(gpu, states, dims, 2, 0.7)
+    _same(got, ref)
