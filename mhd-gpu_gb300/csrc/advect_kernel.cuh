@@ -119,6 +119,7 @@ __device__ __forceinline__ void advect_tile(const AdvectArgs &a, long long tile)
         const int g2 = jc * 5 + (w ? pm : 0);
         const int gk = (j0 + qq) * 5 + (w ? pm : 0);
         const int gb = (j0 + qq) * 3 + (w ? p3 : p2);
+#pragma unroll 4
         for (int i = warp; i < n; i += nwarps) {
             const long long rowc = kb + (long long)i * f.si;
             const long long rowk = kmb + (long long)i * f.si;
@@ -262,14 +263,15 @@ __device__ __forceinline__ void advect_tile(const AdvectArgs &a, long long tile)
         const int p2 = nib(f.pb, 1), p3 = nib(f.pb, 2);
         const int qq = lane >> 2, w = lane & 3;      // 4*ppc <= 32 values per row
         const bool on = lane < 4 * nvalid;
+        // each lane's destination array and stride, chosen once (no divergent
+        // stores in the loop)
+        float *const dst = w == 0 ? a.b + p2 : (w == 1 ? a.b + p3 : (w == 2 ? a.sA : a.sB));
+        const int dstride = w < 2 ? 3 : 1;
+#pragma unroll 4
         for (int i = warp; i < n; i += nwarps) {
             if (!on) continue;
             const long long cell = kb + (long long)i * f.si + j0 + qq;
-            const float v = OUT[i * ro + lane];
-            if (w == 0) a.b[cell * 3 + p2] = v;
-            else if (w == 1) a.b[cell * 3 + p3] = v;
-            else if (w == 2) a.sA[cell] = v;
-            else a.sB[cell] = v;
+            dst[cell * dstride] = OUT[i * ro + lane];
         }
     }
 }

@@ -275,7 +275,12 @@ int build_tables(mhdgpu_batch &bt)
         for (int b = 0; b < g.nb; ++b) {
             const BoxDesc &d = bt.box[g.boxes[b]];
             const Frame f = make_view(axis, d.nx, d.ny, d.nz);
-            fa.push_back(FluidxArgs{d.u, d.u, d.b, &d.clk->dt, &d.clk->health, f});
+            // the step's last sweep (x, fluid last) folds the next step's CFL
+            // reduction into the box's clock word
+            if (g.sweep == 5)
+                fa.push_back(FluidxArgs{d.u, d.u, d.b, &d.clk->dt, &d.clk->health, f, &d.clk->cmax, bt.cfl_mode});
+            else
+                fa.push_back(FluidxArgs{d.u, d.u, d.b, &d.clk->dt, &d.clk->health, f});
             aa.push_back(AdvectArgs{d.b, d.u, &d.clk->dt, d.scr, d.scr + f.npen * f.n, f});
         }
     }
@@ -300,15 +305,20 @@ int build_tables(mhdgpu_batch &bt)
     return MHD_OK;
 }
 
-int launch_step(mhdgpu_batch &bt, cudaStream_t s, cudaEvent_t *ev /* 7 events or NULL */)
+// One step.  With first set the CFL reduction runs as its own pass; otherwise
+// the previous step's last sweep has folded it into the clock words (a max,
+// so a pass over the same state changes nothing).
+int launch_step(mhdgpu_batch &bt, cudaStream_t s, cudaEvent_t *ev /* 7 events or NULL */, bool first)
 {
     const int nb = bt.nbox;
     {
-        ProfScope ps(MHD_KCLASS_CFL, 2, s);
-        CflWork cw{bt.d_box, bt.d_cfl_start, nb, bt.cfl_mode};
-        const int g = (int)std::max(1LL, std::min((long long)bt.num_sms * 8, bt.cfl_total));
-        batch_cfl_kernel<<<g, kCflThreads, 0, s>>>(cw);
-        BCU(cudaGetLastError(), "mhdgpu_batch_advance cfl");
+        ProfScope ps(MHD_KCLASS_CFL, first ? 2 : 1, s);
+        if (first) {
+            CflWork cw{bt.d_box, bt.d_cfl_start, nb, bt.cfl_mode};
+            const int g = (int)std::max(1LL, std::min((long long)bt.num_sms * 8, bt.cfl_total));
+            batch_cfl_kernel<<<g, kCflThreads, 0, s>>>(cw);
+            BCU(cudaGetLastError(), "mhdgpu_batch_advance cfl");
+        }
         const int gc = (std::max(nb, bt.nctr) + 255) / 256;
         batch_clock_kernel<<<gc, 256, 0, s>>>(bt.d_box, bt.d_tf, nb, bt.cfl_number, bt.d_ctr, bt.nctr);
         BCU(cudaGetLastError(), "mhdgpu_batch_advance clock");
@@ -461,7 +471,7 @@ int mhdgpu_batch_advance(mhdgpu_batch *bt, int nsteps, mhdgpu_stream_t stream)
     if (!bt) return bfail(MHD_ERR_ARG, "mhdgpu_batch_advance: null handle");
     if (nsteps < 0) return bfail(MHD_ERR_ARG, "mhdgpu_batch_advance: nsteps < 0");
     for (int it = 0; it < nsteps; ++it) {
-        const int st = launch_step(*bt, (cudaStream_t)stream, nullptr);
+        const int st = launch_step(*bt, (cudaStream_t)stream, nullptr, it == 0);
         if (st) return st;
     }
     return MHD_OK;
@@ -564,7 +574,7 @@ int mhdgpu_batch_tune(mhdgpu_batch *bt, mhdgpu_stream_t stream)
             if (build_tables(*bt) != MHD_OK) continue;   // this schedule does not fit: skip it
             float tsum[3] = {0, 0, 0};
             for (int rep = 0; rep < 3 && st == MHD_OK; ++rep) {
-                st = launch_step(*bt, s, ev);
+                st = launch_step(*bt, s, ev, true);
                 if (st != MHD_OK) break;
                 if ((e = cudaEventSynchronize(ev[6])) != cudaSuccess) { st = bcuda(e, "mhdgpu_batch_tune"); break; }
                 if (rep == 0) continue;   // warm-up

@@ -184,9 +184,22 @@ size_t mhdgpu_step_workspace_bytes(int nx, int ny, int nz)
     return sizeof(float) * 10 * (size_t)nx * ny * nz;
 }
 
+// the last fluid sweep of a step, in place on the x-major state, optionally
+// folding the next step's CFL reduction into it
+static int fluidx_last(float *u, const float *b, int nx, int ny, int nz, const float *dt,
+                       unsigned *health, unsigned *cfl, int cfl_mode, cudaStream_t s)
+{
+    if (!cfl) return mhdgpu_fluidx(u, u, b, nx, ny, nz, dt, health, (mhdgpu_stream_t)s);
+    FluidxArgs a{u, u, b, dt, health, make_frame(nx, ny, nz), cfl, cfl_mode};
+    ProfScope ps(MHD_KCLASS_FLUIDX, 1, s);
+    MHD_CU(launch_fluidx(a, pencil_cfg(MHD_KCLASS_FLUIDX, nx), math_mode(), s), "step fluidx");
+    return MHD_OK;
+}
+
 // one sweep pair in frame (n, a, c): fluid then field, or field then fluid
 static int sweep(float *u, float *b, int n, int a, int c, const float *dt, float *scr,
-                 unsigned *health, bool fluid_first, cudaStream_t s)
+                 unsigned *health, bool fluid_first, cudaStream_t s, unsigned *cfl = nullptr,
+                 int cfl_mode = 0)
 {
     int st;
     if (fluid_first) {
@@ -194,18 +207,31 @@ static int sweep(float *u, float *b, int n, int a, int c, const float *dt, float
         return mhdgpu_advectbyzx(b, u, n, a, c, dt, scr, (mhdgpu_stream_t)s);
     }
     if ((st = mhdgpu_advectbyzx(b, u, n, a, c, dt, scr, (mhdgpu_stream_t)s))) return st;
-    return mhdgpu_fluidx(u, u, b, n, a, c, dt, health, (mhdgpu_stream_t)s);
+    return fluidx_last(u, b, n, a, c, dt, health, cfl, cfl_mode, s);
 }
+
+static int step_plain(float *u, float *b, int nx, int ny, int nz, const float *d_dt, void *d_work,
+                      unsigned *d_health, cudaStream_t s, unsigned *cfl, int cfl_mode);
+static int step_fused(float *u, float *b, int nx, int ny, int nz, const float *d_dt, void *d_work,
+                      unsigned *d_health, cudaStream_t s, unsigned *cfl, int cfl_mode);
 
 int mhdgpu_step(float *u, float *b, int nx, int ny, int nz, const float *d_dt, void *d_work,
                 unsigned *d_health, mhdgpu_stream_t stream)
 {
+    return step_plain(u, b, nx, ny, nz, d_dt, d_work, d_health, (cudaStream_t)stream, nullptr, 0);
+}
+
+// the plain step; with cfl set, its last fluid sweep also folds the next
+// step's CFL fast speeds into *cfl (mode cfl_mode)
+static int step_plain(float *u, float *b, int nx, int ny, int nz, const float *d_dt, void *d_work,
+                      unsigned *d_health, cudaStream_t s, unsigned *cfl, int cfl_mode)
+{
+    const mhdgpu_stream_t stream = (mhdgpu_stream_t)s;
     int st = check_dims(nx, ny, nz, "mhdgpu_step");
     if (st) return st;
     if (ny > MHD_MAX_PENCIL || nz > MHD_MAX_PENCIL)
         return fail(MHD_ERR_ARG, "mhdgpu_step: every axis becomes a pencil; each must be <= MHD_MAX_PENCIL");
     if (!u || !b || !d_dt || !d_work) return fail(MHD_ERR_ARG, "mhdgpu_step: null pointer");
-    cudaStream_t s = (cudaStream_t)stream;
     const size_t ncell = (size_t)nx * ny * nz;
     float *u2 = (float *)d_work;
     float *b2 = u2 + 5 * ncell;
@@ -224,16 +250,17 @@ int mhdgpu_step(float *u, float *b, int nx, int ny, int nz, const float *d_dt, v
     if ((st = sweep(u2, b2, ny, nx, nz, d_dt, scr, d_health, false, s))) return st;
     // x back
     if ((st = mhdgpu_transpose12(u, b, u2, b2, ny, nx, nz, stream))) return st;
-    return sweep(u, b, nx, ny, nz, d_dt, scr, d_health, false, s);
+    return sweep(u, b, nx, ny, nz, d_dt, scr, d_health, false, s, cfl, cfl_mode);
 }
 
 // one sweep pair on a frame view of the x-major state: fluid then field, or
 // field then fluid; launches the kernels on the view directly
 static int sweep_view(float *u, float *b, const Frame &f, const float *dt, float *scr,
-                      unsigned *health, bool fluid_first, cudaStream_t s)
+                      unsigned *health, bool fluid_first, cudaStream_t s, unsigned *cfl = nullptr,
+                      int cfl_mode = 0)
 {
     const long long ncell = f.npen * f.n;
-    FluidxArgs fa{u, u, b, dt, health, f};
+    FluidxArgs fa{u, u, b, dt, health, f, cfl, cfl_mode};
     AdvectArgs aa{b, u, dt, scr, scr + ncell, f};
     for (int part = 0; part < 2; ++part) {
         if ((part == 0) == fluid_first) {
@@ -258,12 +285,17 @@ size_t mhdgpu_step_fused_workspace_bytes(int nx, int ny, int nz)
 int mhdgpu_step_fused(float *u, float *b, int nx, int ny, int nz, const float *d_dt, void *d_work,
                       unsigned *d_health, mhdgpu_stream_t stream)
 {
+    return step_fused(u, b, nx, ny, nz, d_dt, d_work, d_health, (cudaStream_t)stream, nullptr, 0);
+}
+
+static int step_fused(float *u, float *b, int nx, int ny, int nz, const float *d_dt, void *d_work,
+                      unsigned *d_health, cudaStream_t s, unsigned *cfl, int cfl_mode)
+{
     int st = check_dims(nx, ny, nz, "mhdgpu_step_fused");
     if (st) return st;
     if (ny > MHD_MAX_PENCIL || nz > MHD_MAX_PENCIL)
         return fail(MHD_ERR_ARG, "mhdgpu_step_fused: every axis becomes a pencil; each must be <= MHD_MAX_PENCIL");
     if (!u || !b || !d_dt || !d_work) return fail(MHD_ERR_ARG, "mhdgpu_step_fused: null pointer");
-    cudaStream_t s = (cudaStream_t)stream;
     float *scr = (float *)d_work;
     const Frame fx = make_view(0, nx, ny, nz), fy = make_view(1, nx, ny, nz), fz = make_view(2, nx, ny, nz);
     if ((st = sweep_view(u, b, fx, d_dt, scr, d_health, true, s))) return st;
@@ -271,7 +303,7 @@ int mhdgpu_step_fused(float *u, float *b, int nx, int ny, int nz, const float *d
     if ((st = sweep_view(u, b, fz, d_dt, scr, d_health, true, s))) return st;
     if ((st = sweep_view(u, b, fz, d_dt, scr, d_health, false, s))) return st;
     if ((st = sweep_view(u, b, fy, d_dt, scr, d_health, false, s))) return st;
-    return sweep_view(u, b, fx, d_dt, scr, d_health, false, s);
+    return sweep_view(u, b, fx, d_dt, scr, d_health, false, s, cfl, cfl_mode);
 }
 
 int mhdgpu_advance(float *u, float *b, int nx, int ny, int nz, int nsteps, double cfl_number,
@@ -286,15 +318,21 @@ int mhdgpu_advance(float *u, float *b, int nx, int ny, int nz, int nsteps, doubl
     if (path != MHD_PATH_PLAIN && path != MHD_PATH_FUSED)
         return fail(MHD_ERR_ARG, "mhdgpu_advance: bad path");
     cudaStream_t s = (cudaStream_t)stream;
+    // The CFL reduction runs as its own pass before the first step of the
+    // call; every step's last fluid sweep folds the next step's reduction into
+    // the clock's word (a max, so the first pass of a later call, over the
+    // same state, changes nothing).
     for (int it = 0; it < nsteps; ++it) {
         {
-            ProfScope ps(MHD_KCLASS_CFL, 2, s);
-            MHD_CU(launch_cfl(u, b, nx, ny, nz, cfl_mode, &d_clock->cmax, s), "mhdgpu_advance");
+            ProfScope ps(MHD_KCLASS_CFL, it == 0 ? 2 : 1, s);
+            if (it == 0) MHD_CU(launch_cfl(u, b, nx, ny, nz, cfl_mode, &d_clock->cmax, s), "mhdgpu_advance");
             MHD_CU(launch_clock(d_clock, cfl_number, tf, d_dt_log, s), "mhdgpu_advance");
         }
         int st = (path == MHD_PATH_FUSED)
-                     ? mhdgpu_step_fused(u, b, nx, ny, nz, &d_clock->dt, d_work, &d_clock->health, stream)
-                     : mhdgpu_step(u, b, nx, ny, nz, &d_clock->dt, d_work, &d_clock->health, stream);
+                     ? step_fused(u, b, nx, ny, nz, &d_clock->dt, d_work, &d_clock->health, s, &d_clock->cmax,
+                                  cfl_mode)
+                     : step_plain(u, b, nx, ny, nz, &d_clock->dt, d_work, &d_clock->health, s, &d_clock->cmax,
+                                  cfl_mode);
         if (st) return st;
     }
     return MHD_OK;

@@ -34,23 +34,6 @@ __device__ __forceinline__ float cfl_cell_speed(const float *__restrict__ u, con
     return cfl_speed_averaged(uu, bb);
 }
 
-// max over the CTA, then one atomicMax on the float's bit pattern (monotone
-// for non-negative floats); every thread of the CTA must call it
-__device__ __forceinline__ void cfl_block_max(float cl, unsigned *cmax)
-{
-    __shared__ float red[32];
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) cl = fmaxf(cl, __shfl_xor_sync(0xffffffffu, cl, o));
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = cl;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        float r = red[0];
-        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) r = fmaxf(r, red[w]);
-        atomicMax(cmax, __float_as_uint(r));
-    }
-    __syncthreads();
-}
-
 // dt = cfl*(1/c) in double rounded to float; clamp to (tf-t)/2 (C/mhd.c:63-64)
 __device__ __forceinline__ float dt_rule(float inv_c, double cfl_number, float t, float tf)
 {

@@ -100,6 +100,7 @@ __device__ __forceinline__ void fluidx_tile(const FluidxArgs &a, long long tile)
 
     // ---- stage u (kept) and b (transient) ----
     float bc[CPL][3];
+    const float *bjp = nullptr, *bkp = nullptr;   // !ROWS: b of the j+1 and k+1 pencils
     if (!ROWS) {
         block_copy_in(US, a.u_in + p0 * 5 * n, (long long)nvalid * 5 * n, threadIdx.x, blockDim.x);
         block_copy_in(XA, a.b + p0 * 3 * n, (long long)nvalid * 3 * n, threadIdx.x, blockDim.x);
@@ -110,8 +111,8 @@ __device__ __forceinline__ void fluidx_tile(const FluidxArgs &a, long long tile)
         // kernel writes b earlier in the same launch.
         const int jp = (jq + 1 == f.ny) ? 0 : jq + 1;
         const int kp = (kq + 1 == f.nz) ? 0 : kq + 1;
-        const float *bjp = a.b + ((long long)kq * f.ny + jp) * 3 * n;
-        const float *bkp = a.b + ((long long)kp * f.ny + jq) * 3 * n;
+        bjp = a.b + ((long long)kq * f.ny + jp) * 3 * n;
+        bkp = a.b + ((long long)kp * f.ny + jq) * 3 * n;
         const float *pb = XA + (size_t)q * 3 * n;
 #pragma unroll
         for (int m = 0; m < CPL; ++m) {
@@ -154,6 +155,7 @@ __device__ __forceinline__ void fluidx_tile(const FluidxArgs &a, long long tile)
             gb_off[h] = j * 3 + pp;
         }
         const bool sk_on = lane < nvalid;
+#pragma unroll 4
         for (int i = warp; i < n; i += nwarps) {
             const long long rowc = kb + (long long)i * f.si;    // cell of (i, 0, k)
             const float *gu = a.u_in + (rowc + j0) * 5;
@@ -297,22 +299,44 @@ __device__ __forceinline__ void fluidx_tile(const FluidxArgs &a, long long tile)
         tm.sync();
         // u = u - (flux - cshift(flux,-1)) dt, written back into US
         const float mdt = -dt;
+        const bool fold_cfl = !ROWS && a.cfl != nullptr;
+        const float *bown = a.b + (p0 + q) * 3 * n;   // !ROWS: this pencil's b
+        float cfl_c = 0.0f;
 #pragma unroll
         for (int m = 0; m < CPL; ++m) {
             if (!(live && tm.valid(m))) continue;
             const int cc = tm.ci(m);
             float s = 0.0f, r = 0.0f;
+            float uf[5];
 #pragma unroll
             for (int ii = 0; ii < 5; ++ii) {
                 const float d = M::sub(fx[m][ii], X(ii)[cc - 1]);
                 const float un = M::add(us[cc * 5 + ii], M::mul(mdt, d));
                 us[cc * 5 + ii] = un;
+                uf[ii] = un;
                 s += un;
                 if (ii == 0) r = un;
             }
             if (!(r > 0.0f)) bad |= MHD_HEALTH_DENSITY;
             if (!isfinite(s)) bad |= MHD_HEALTH_NONFINITE;
+            if (fold_cfl) {
+                // the CFL fast speed of the updated cell, as cfl_cell_speed forms it
+                float bb[3];
+                if (a.cfl_mode == MHD_CFL_C) {
+                    bb[0] = bown[cc * 3 + 0];
+                    bb[1] = bown[cc * 3 + 1];
+                    bb[2] = bown[cc * 3 + 2];
+                    cfl_c = fmaxf(cfl_c, cfl_speed_c(uf, bb));
+                } else {
+                    const int cp = (cc + 1 == n) ? 0 : cc + 1;
+                    bb[0] = fdiv(fadd(bown[cc * 3 + 0], bown[cp * 3 + 0]), 2.0f);
+                    bb[1] = fdiv(fadd(bown[cc * 3 + 1], bjp[cc * 3 + 1]), 2.0f);
+                    bb[2] = fdiv(fadd(bown[cc * 3 + 2], bkp[cc * 3 + 2]), 2.0f);
+                    cfl_c = fmaxf(cfl_c, cfl_speed_averaged(uf, bb));
+                }
+            }
         }
+        if (fold_cfl) cfl_block_max(cfl_c, a.cfl);   // every thread of the CTA (a.cfl is uniform)
     }
 
     if (!live) bad = 0;
@@ -332,6 +356,7 @@ __device__ __forceinline__ void fluidx_tile(const FluidxArgs &a, long long tile)
             const int qq = r / 5, p = r - qq * 5;
             off[h] = qq * ps + nib(f.iu, p);
         }
+#pragma unroll 4
         for (int i = warp; i < n; i += nwarps) {
             float *g = a.u_out + (kb + (long long)i * f.si + j0) * 5;
 #pragma unroll

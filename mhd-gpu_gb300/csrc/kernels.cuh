@@ -15,6 +15,12 @@ struct FluidxArgs {
     const float *dt;
     unsigned *health;
     Frame f;
+    // Optional, contiguous identity frames only (the last x sweep of a step):
+    // fold the updated cells' CFL fast speed (mode MHD_CFL_C or
+    // MHD_CFL_AVERAGED) into *cfl with atomicMax, which saves the next step's
+    // reduction pass over the state.
+    unsigned *cfl = nullptr;
+    int cfl_mode = 0;
 };
 
 struct AdvectArgs {

@@ -143,6 +143,24 @@ struct Team {
     }
 };
 
+// max over the CTA of non-negative values, then one atomicMax of the float's
+// bit pattern (monotone for non-negative floats); NaN is dropped as the
+// reference's strict '>' scan drops it.  Every thread of the CTA calls it.
+__device__ __forceinline__ void cfl_block_max(float cl, unsigned *cmax)
+{
+    __shared__ float red[32];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) cl = fmaxf(cl, __shfl_xor_sync(0xffffffffu, cl, o));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = cl;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float r = red[0];
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) r = fmaxf(r, red[w]);
+        atomicMax(cmax, __float_as_uint(r));
+    }
+    __syncthreads();
+}
+
 // Device health word bits (also in include/mhdgpu.h).
 __device__ __forceinline__ void flag_health(unsigned *health, unsigned bits)
 {

@@ -141,16 +141,17 @@ struct Faithful {
     MHD_HD static float twice_plus(float v, float s) { return ffma(2.0f, v, s); }
     // RN(b - p/2) formed once (the reference's double b - p/2.0)
     MHD_HD static float minus_half(float b, float p) { return ffma(-0.5f, p, b); }
+    // (branch-free: where XY <= 0 the quotient is formed and discarded)
     MHD_HD static float slope(float X, float Y)
     {
         const float ph = fmul(X, Y);
-        if (!(ph > 0.0f)) return 0.0f;
         const float pl = ffma(X, Y, -ph);
         const float s = fadd(X, Y);
         const float y = rcp_approx(s);
         const float q0 = fmul(ph, y);
         const float e = fadd(ffma(-q0, s, ph), pl);
-        return ffma(e, y, q0);
+        const float q = ffma(e, y, q0);
+        return (ph > 0.0f) ? q : 0.0f;
     }
     MHD_HD static float pressure(float e, float q, float b2) { return total_pressure(e, q, b2); }
     // total pressure ps (mhdflux.c:26-29) and gas pressure p = ps - B^2/2
