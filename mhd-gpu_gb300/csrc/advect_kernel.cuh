@@ -46,7 +46,7 @@ __host__ __device__ inline long long ax_smem_floats(int n, int ppc, bool rows)
 template <int CPL, int WPP, class M, bool ROWS, int NT>
 __device__ __forceinline__ void advect_tile(const AdvectArgs &a, long long tile)
 {
-    constexpr int TPP = 32 * WPP;
+    constexpr int TPP = team_threads<WPP>();
     extern __shared__ float smem[];
     const Frame &f = a.f;
     const int n = NT > 0 ? NT : f.n;
@@ -119,7 +119,6 @@ __device__ __forceinline__ void advect_tile(const AdvectArgs &a, long long tile)
         const int g2 = jc * 5 + (w ? pm : 0);
         const int gk = (j0 + qq) * 5 + (w ? pm : 0);
         const int gb = (j0 + qq) * 3 + (w ? p3 : p2);
-#pragma unroll 4
         for (int i = warp; i < n; i += nwarps) {
             const long long rowc = kb + (long long)i * f.si;
             const long long rowk = kmb + (long long)i * f.si;
@@ -267,7 +266,6 @@ __device__ __forceinline__ void advect_tile(const AdvectArgs &a, long long tile)
         // stores in the loop)
         float *const dst = w == 0 ? a.b + p2 : (w == 1 ? a.b + p3 : (w == 2 ? a.sA : a.sB));
         const int dstride = w < 2 ? 3 : 1;
-#pragma unroll 4
         for (int i = warp; i < n; i += nwarps) {
             if (!on) continue;
             const long long cell = kb + (long long)i * f.si + j0 + qq;

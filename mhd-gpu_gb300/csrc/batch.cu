@@ -80,6 +80,7 @@ struct BatchGroup {
     long long cells = 0, items = 0;
     size_t smem = 0;
     int grid = 1;
+    int threads = 256;            // CTA size of the launch
 };
 
 struct mhdgpu_batch {
@@ -232,8 +233,10 @@ int build_tables(mhdgpu_batch &bt)
     for (BatchGroup &g : bt.groups) {
         const int axis = kSweepAxis[g.sweep];
         const bool rows = axis != 0;
-        const int threads = bt.threads[axis];
+        // at most 8 pencils per CTA (the row staging's lane layout)
         const int tpp = batch_class_tpp(g.cls);
+        const int threads = std::min(bt.threads[axis], 8 * tpp);
+        g.threads = threads;
         const int ppc = threads / tpp;
         if (ppc < 1)
             return bfail(MHD_ERR_ARG, "mhdgpu_batch: fewer threads per CTA than a pencil's team "
@@ -293,7 +296,7 @@ int build_tables(mhdgpu_batch &bt)
         const int axis = kSweepAxis[s];
         for (int gi = bt.gbegin[s]; gi < bt.gbegin[s + 1]; ++gi) {
             BatchGroup &g = bt.groups[gi];
-            const int occ = occupancy(g.cls, axis != 0, bt.threads[axis], g.smem);
+            const int occ = occupancy(g.cls, axis != 0, g.threads, g.smem);
             if (occ < 1) return bfail(MHD_ERR_CUDA, "mhdgpu_batch: a class kernel cannot be resident");
             g.grid = (int)std::max(1LL, std::min((long long)bt.num_sms * std::min(bt.cps[axis], occ), g.items));
         }
@@ -348,7 +351,7 @@ int launch_step(mhdgpu_batch &bt, cudaStream_t s, cudaEvent_t *ev /* 7 events or
                 gs = bt.side[(gi - g0) % kBatchClasses];
                 BCU(cudaStreamWaitEvent(gs, bt.fork, 0), "mhdgpu_batch fork");
             }
-            BCU(launch_group(w, g.cls, axis != 0, g.grid, bt.threads[axis], g.smem, gs), "mhdgpu_batch_advance sweep");
+            BCU(launch_group(w, g.cls, axis != 0, g.grid, g.threads, g.smem, gs), "mhdgpu_batch_advance sweep");
             if (fan) {
                 BCU(cudaEventRecord(bt.join[(gi - g0) % kBatchClasses], gs), "mhdgpu_batch join");
                 BCU(cudaStreamWaitEvent(s, bt.join[(gi - g0) % kBatchClasses], 0), "mhdgpu_batch join");

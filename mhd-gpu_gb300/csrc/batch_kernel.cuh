@@ -48,7 +48,7 @@ struct BoxDesc {
 
 // team class by pencil length (1 <= n <= kBatchMaxPencil):
 //   0: 32 = 1 x 32 threads     1: 64 = 2 x 32      2: 96 = 3 x 32
-//   3: 128 = 4 x 32            4: 48 (2 x 32, 16 slots idle)
+//   3: 128 = 4 x 32            4: 48 = 3 x 16 (half-warp teams)
 //   5: other n < 64 (2 x 32)   6: other n < 128 (2 x 64)   7: n <= 256 (2 x 128)
 __host__ __device__ inline int batch_class(int n)
 {
@@ -62,7 +62,10 @@ __host__ __device__ inline int batch_class(int n)
     }
 }
 // threads per pencil of a class
-__host__ __device__ inline int batch_class_tpp(int c) { return c == 6 ? 64 : (c == 7 ? 128 : 32); }
+__host__ __device__ inline int batch_class_tpp(int c)
+{
+    return c == 4 ? 16 : (c == 6 ? 64 : (c == 7 ? 128 : 32));
+}
 __host__ __device__ inline int batch_tpp(int n) { return batch_class_tpp(batch_class(n)); }
 
 // items of a phase: tiles of ppc pencils (contiguous pencils are numbered
@@ -202,7 +205,7 @@ batch_class_kernel(const __grid_constant__ ClassWork w)
             if (ph == kPhaseB1) {
                 batch_b1(w.aa[bx], local * g, g);
             } else {
-                const int ppc = blockDim.x / (32 * WPP);
+                const int ppc = blockDim.x / team_threads<WPP>();
                 const long long t0 = local * g;
                 const long long t1 = min(t0 + g, batch_tiles(w.fa[bx].f, ppc, ROWS));
                 for (long long t = t0; t < t1; ++t) {
@@ -219,10 +222,11 @@ batch_class_kernel(const __grid_constant__ ClassWork w)
 }
 
 // the classes: (class, cells per thread, warps per pencil, compile-time
-// length, CTAs per SM the registers are bounded for).  The full-team classes
-// fit 64 registers without spilling; uncapped, the compiler spends up to 128.
+// length, CTAs per SM the registers are bounded for; warps per pencil 0 is a
+// half-warp team).  The full-team classes fit 64 registers without spilling;
+// uncapped, the compiler spends up to 128.
 #define MHD_BATCH_CLASSES(X)                                                           \
-    X(0, 1, 1, 32, 4) X(1, 2, 1, 64, 4) X(2, 3, 1, 96, 4) X(3, 4, 1, 128, 4) X(4, 2, 1, 48, 3) \
+    X(0, 1, 1, 32, 4) X(1, 2, 1, 64, 4) X(2, 3, 1, 96, 4) X(3, 4, 1, 128, 4) X(4, 3, 0, 48, 4) \
     X(5, 2, 1, 0, 2) X(6, 2, 2, 0, 2) X(7, 2, 4, 0, 2)
 
 template <class M, bool ROWS>

@@ -58,7 +58,7 @@ __host__ __device__ inline long long fx_smem_floats(int n, int ppc, int wpp, boo
 template <int CPL, int WPP, class M, bool ROWS, int NT>
 __device__ __forceinline__ void fluidx_tile(const FluidxArgs &a, long long tile)
 {
-    constexpr int TPP = 32 * WPP;
+    constexpr int TPP = team_threads<WPP>();
     extern __shared__ float smem[];
     const Frame &f = a.f;
     const int n = NT > 0 ? NT : f.n;
@@ -155,7 +155,6 @@ __device__ __forceinline__ void fluidx_tile(const FluidxArgs &a, long long tile)
             gb_off[h] = j * 3 + pp;
         }
         const bool sk_on = lane < nvalid;
-#pragma unroll 4
         for (int i = warp; i < n; i += nwarps) {
             const long long rowc = kb + (long long)i * f.si;    // cell of (i, 0, k)
             const float *gu = a.u_in + (rowc + j0) * 5;
@@ -356,7 +355,6 @@ __device__ __forceinline__ void fluidx_tile(const FluidxArgs &a, long long tile)
             const int qq = r / 5, p = r - qq * 5;
             off[h] = qq * ps + nib(f.iu, p);
         }
-#pragma unroll 4
         for (int i = warp; i < n; i += nwarps) {
             float *g = a.u_out + (kb + (long long)i * f.si + j0) * 5;
 #pragma unroll

@@ -70,7 +70,12 @@ __host__ __device__ inline bool frame_rows(const Frame &f)
     return !(f.si == 1 && f.pu == 0x43210u && f.pb == 0x210u);
 }
 
-// A team of TPP = 32*WPP threads owns one pencil; thread t holds the CPL
+// threads of a pencil team: WPP warps, or half a warp for WPP = 0
+template <int WPP>
+__host__ __device__ constexpr int team_threads() { return WPP == 0 ? 16 : 32 * WPP; }
+
+// A team of TPP = 32*WPP threads (16 for WPP = 0: two teams share a warp)
+// owns one pencil; thread t holds the CPL
 // cells c = m*TPP + t (m < CPL).  Cells >= n are padding: they compute on
 // harmless values and are never reduced or stored.  NT > 0 is the pencil
 // length known at compile time; when it equals the team's capacity (FULL)
@@ -82,7 +87,7 @@ __host__ __device__ inline bool frame_rows(const Frame &f)
 // their periodic copies at -1, n and n+1.  A row takes rs() = n+3 floats.
 template <int CPL, int WPP, int NT = 0>
 struct Team {
-    static constexpr int TPP = 32 * WPP;
+    static constexpr int TPP = team_threads<WPP>();
     static constexpr bool FULL = NT > 0 && NT == TPP * CPL;
     int t;      // thread within the team
     int n;      // pencil length
@@ -121,7 +126,7 @@ struct Team {
     // a CTA runs the same phase sequence, so a CTA barrier is correct).
     __device__ __forceinline__ void sync() const
     {
-        if (WPP == 1) __syncwarp();
+        if (WPP <= 1) __syncwarp();   // a half-warp team's partner runs the same sequence
         else __syncthreads();
     }
 
@@ -130,8 +135,8 @@ struct Team {
     __device__ float pencil_max(float x, float *red) const
     {
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) x = fmaxf(x, __shfl_xor_sync(0xffffffffu, x, o));
-        if (WPP == 1) return x;
+        for (int o = (TPP < 32 ? TPP : 32) / 2; o > 0; o >>= 1) x = fmaxf(x, __shfl_xor_sync(0xffffffffu, x, o));
+        if (WPP <= 1) return x;
         const int w = t >> 5;
         if ((t & 31) == 0) red[w] = x;
         __syncthreads();
