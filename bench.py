@@ -54,6 +54,11 @@ FLUIDX_BYTES_PER_CELL = 52      # R u 20 + b 12, W u 20 (one read and write of t
 # R b2 b3 8, W b2 b3 8, W sA sB 8); b(1) 16 (R sA sB 8, R+W b1 8)
 SWEEP_BYTES_PER_CELL = 100
 STEP_BYTES_64 = 64              # one read + one write of the 8-float state per cell-update
+# floating-point operations per cell-update of one full step (6 fluid and 6 field
+# sweeps + the CFL reduction), counted on the oracle as the reference writes
+# them (oracle/flopcount.cpp, 64^3: fluidx 579.7 and advectbyzx 60.0 per
+# cell-sweep, CFL 40.0 per step)
+FLOPS_PER_CELL_UPDATE = 3878
 PLAIN_PASS_BYTES = 792          # minimal per-subroutine pass bytes per cell-update
 ENSEMBLE = {"nbox": 64, "seed": 0, "sizes": (32, 48, 64, 96, 128), "amp_range": (1e-4, 1e-1)}
 CFL = 0.7
@@ -125,6 +130,26 @@ class ClockSampler:
         return {"sm_mhz": statistics.median(r[1] for r in inside),
                 "sm_max_mhz": max(r[2] for r in inside), "reasons": reasons,
                 "samples": len(inside)}
+
+
+def roofline_step(value, world, hbm, dev, clocks, pass_bytes):
+    """The whole step against both roofs: HBM at the 64 B/cell-update basis and
+    at the path's own pass bytes, and FP32 issue at the counted flops."""
+    import torch
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    mhz = clocks.get("sm_max_mhz") or 2070.0
+    fp32_peak = sms * 128 * 2 * mhz * 1e6 / 1e12        # FMA = 2 flops, 128 FP32 lanes per SM
+    per_gpu = value / world
+    return {"bytes_per_cell_update_64B_basis": STEP_BYTES_64,
+            "frac_64B_basis": per_gpu * STEP_BYTES_64 / 1e9 / hbm,
+            "pass_bytes_per_cell_update": pass_bytes,
+            "frac_pass_bytes": per_gpu * pass_bytes / 1e9 / hbm,
+            "flops_per_cell_update": FLOPS_PER_CELL_UPDATE,
+            "flops_source": "oracle/flopcount.cpp (every +,-,*,/,sqrt of the restatement)",
+            "tflops": per_gpu * FLOPS_PER_CELL_UPDATE / 1e12,
+            "fp32_peak_tflops": fp32_peak,
+            "fp32_peak_source": f"nominal: {sms} SMs x 128 lanes x 2 x {mhz:.0f} MHz",
+            "frac_fp32_peak": per_gpu * FLOPS_PER_CELL_UPDATE / 1e12 / fp32_peak}
 
 
 def read_traffic(name):
@@ -564,8 +589,8 @@ def main():
             "dtype": "f32", "data": "synthetic (seeded ensemble, see config)", "config": config,
             "gpu_launches": int(round(sum(launches.values()) * K)),
             "roofline": out_roof,
-            "roofline_step": {"bytes_per_cell_update_64B_basis": STEP_BYTES_64,
-                              "frac_64B_basis": value * STEP_BYTES_64 / 1e9 / world / out_roof["peak"]},
+            "roofline_step": roofline_step(value, world, out_roof["peak"], dev, clocks,
+                                           SWEEP_BYTES_PER_CELL * 6),
             "plain_drop_in": {"value": eb["boxwise_plain"]["value"], "unit": UNIT,
                               "ms_per_step": eb["boxwise_plain"]["ms_per_step"],
                               "path": eb["boxwise_plain"]["path"]},
@@ -585,10 +610,8 @@ def main():
             "data": "synthetic (seedless analytic initial state, see config.ic)", "config": config,
             "gpu_launches": int(round(sum(fused["kernel_launches_per_step"].values()) * K)),
             "roofline": sb["fluidx_roofline"],
-            "roofline_step": {"bytes_per_cell_update_64B_basis": STEP_BYTES_64,
-                              "frac_64B_basis": fused["value"] * STEP_BYTES_64 / 1e9 / world
-                              / sb["fluidx_roofline"]["peak"],
-                              "plain_pass_bytes_per_cell_update": PLAIN_PASS_BYTES},
+            "roofline_step": roofline_step(fused["value"], world, sb["fluidx_roofline"]["peak"], dev, clocks,
+                                           SWEEP_BYTES_PER_CELL * 6),
             "plain_drop_in": {"value": sb["plain"]["value"], "unit": UNIT,
                               "ms_per_step": sb["plain"]["ms_per_step"], "path": sb["plain"]["path"]},
             "fused_over_plain": sb["fused_over_plain"],

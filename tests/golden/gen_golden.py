@@ -6,9 +6,9 @@
 Every output here is computed by the reference's own C path
 (Heterogeneous_MHD/C/*.c compiled unmodified into oracle/_ref/libref_*.so),
 driven in the order of Heterogeneous_MHD/C/mhd.c:60-125.  The inputs are
-  - the reference's shipped initial state data/source_init_alfvenlinear_16cube.dat
-    (raw little-endian float32, 8 per cell, read into C index order i, j, k
-    as Heterogeneous_MHD/C/init.c:33-54 does), and
+  - the reference's shipped initial states data/source_init_alfvenlinear_16cube.dat
+    and _32cube.dat (raw little-endian float32, 8 per cell, read into C index
+    order i, j, k as Heterogeneous_MHD/C/init.c:33-54 does), and
   - seeded random physical states (mhd-gpu_gb300/ics.py random_state).
 The fixtures carry their inputs, so checking them needs neither the
 reference checkout nor the reference build.
@@ -67,16 +67,37 @@ def write_digest(ref):
         f.write(f"{hashlib.sha256(raw).hexdigest()} {len(raw)}\n")
 
 
+def write_alfven32(ref, R):
+    """The shipped 32^3 state run by the reference to tf = 4*nx = 128 at CFL
+    0.9: the input, the dt sequence, sha256 digests of the final u and b, and
+    every 97th value of them (the fixture stays small; the oracle must match
+    the digests bit for bit)."""
+    import hashlib
+    u0, b0 = read_dat(os.path.join(ref, "data", "source_init_alfvenlinear_32cube.dat"), 32)
+    uf, bf = u0.copy(), b0.copy()
+    sf, tfin, dtsf = R.run(uf, bf, 32, 32, 32, cfl_number=0.9, tf=128.0, max_steps=100000)
+    np.savez_compressed(os.path.join(HERE, "alfven32_dat.npz"), u0=u0, b0=b0, dtsf=dtsf,
+                        steps=np.array([sf]), t=np.array([tfin], dtype=np.float32),
+                        uf_sha=np.array([hashlib.sha256(uf.tobytes()).hexdigest()]),
+                        bf_sha=np.array([hashlib.sha256(bf.tobytes()).hexdigest()]),
+                        uf_sample=uf[::97].copy(), bf_sample=bf[::97].copy())
+    print("alfven32_dat: steps", sf, "t", tfin)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default=os.environ.get("MHD_REFERENCE", "/root/reference"))
     ap.add_argument("--only-digest", action="store_true")
+    ap.add_argument("--only-alfven32", action="store_true")
     args = ap.parse_args()
     write_digest(args.ref)
     if args.only_digest:
         return
     R = O.reference("f32")
     R64 = O.reference("f64")
+    write_alfven32(args.ref, R)
+    if args.only_alfven32:
+        return
 
     # 1. shipped 16^3 Alfven state: 1 step and the reference's full run to tf = 4*nx
     u0, b0 = read_dat(os.path.join(args.ref, "data", "source_init_alfvenlinear_16cube.dat"), 16)

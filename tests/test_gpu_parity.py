@@ -220,6 +220,24 @@ def test_shipped_alfven_state_full_run_matches_reference(gpu, path):
 
 
 @pytest.mark.parametrize("path", PATHS)
+def test_shipped_32cube_state_full_run_matches_reference(gpu, path):
+    """The reference's own run from data/source_init_alfvenlinear_32cube.dat:
+    108 steps to tf = 128 at CFL 0.9.  The fixture carries digests of the final
+    state and every 97th value; the faithful kernels reproduce the digests."""
+    import hashlib
+    g = np.load(os.path.join(GOLD, "alfven32_dat.npz"))
+    gu, gb, dts, clk = _advance(gpu, g["u0"], g["b0"], 32, 32, 32, 120, 0.9, tf=128.0, path=path)
+    assert clk.iter == 108
+    assert clk.health & (gpu.MHD_HEALTH_NONFINITE | gpu.MHD_HEALTH_DENSITY) == 0
+    assert np.array_equal(dts, g["dtsf"])
+    eu = field_errors(gu[::97], g["uf_sample"], 1, vector_floor=False)
+    eb = field_errors(gb[::97], g["bf_sample"], 1, vector_floor=False)
+    assert max(eu) < TOL and max(eb) < TOL, (eu, eb)
+    assert hashlib.sha256(gu.tobytes()).hexdigest() == str(g["uf_sha"][0])
+    assert hashlib.sha256(gb.tobytes()).hexdigest() == str(g["bf_sha"][0])
+
+
+@pytest.mark.parametrize("path", PATHS)
 def test_config1_alfven_x_32_100_steps(gpu, oracle_lib, path):
     """32^3 Alfven wave along x, A=1e-3, CFL 0.7, 100 steps."""
     import ics

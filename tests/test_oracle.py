@@ -137,3 +137,34 @@ def test_oracle_bit_exact_against_reference_build(oracle_lib):
                 u, b = uu, bb
             out.append((u, b))
         assert bits_equal(out[0][0], out[1][0]) and bits_equal(out[0][1], out[1][1]), dims
+
+
+def test_flop_count_per_cell_update(oracle_lib):
+    """The operation count of one step (oracle/flopcount.cpp: every +, -, *, /
+    and sqrt of the restatement as the reference writes them) is the figure the
+    roofline's flop rate uses (bench.py FLOPS_PER_CELL_UPDATE)."""
+    import subprocess
+    import sys
+    repo = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    sys.path.insert(0, repo)
+    import bench
+    odir = os.path.join(repo, "oracle")
+    subprocess.run(["make", "-s", "-C", odir, "flopcount"], check=True)
+    out = subprocess.run([os.path.join(odir, "lib", "flopcount"), "64", "64", "64"], check=True,
+                         capture_output=True, text=True).stdout
+    total = float(out.split("flops per cell-update:")[1].split()[0])
+    assert abs(total - bench.FLOPS_PER_CELL_UPDATE) < 5, (total, out)
+
+
+def test_oracle_matches_reference_run_on_shipped_32cube_state(oracle_lib):
+    """108 steps to tf = 128 from data/source_init_alfvenlinear_32cube.dat at
+    CFL 0.9: the reference's own run, bit for bit (digests of the final state)."""
+    import hashlib
+    O = oracle_lib.oracle("f32")
+    g = np.load(os.path.join(GOLD, "alfven32_dat.npz"))
+    u, b = g["u0"].copy(), g["b0"].copy()
+    s, t, dts = O.run(u, b, 32, 32, 32, cfl_number=0.9, tf=128.0, max_steps=100000)
+    assert s == int(g["steps"][0]) == 108
+    assert bits_equal(dts, g["dtsf"])
+    assert hashlib.sha256(u.tobytes()).hexdigest() == str(g["uf_sha"][0])
+    assert hashlib.sha256(b.tobytes()).hexdigest() == str(g["bf_sha"][0])
