@@ -9,7 +9,8 @@ Workloads (synthetic inputs, mhd-gpu_gb300/ics.py):
     (27.2 M cells, 0.87 GB of state), each a linear Alfven wave on the box
     diagonal or a turbulent start with an amplitude drawn log-uniformly from
     [1e-4, 1e-1]; CFL 0.7, C-path CFL formula.  The batched path
-    (mhdgpu_batch_*) advances all boxes with one persistent launch per sweep;
+    (mhdgpu_batch_*) advances all boxes together: per sweep, one persistent
+    launch per pencil-length class, the classes concurrent;
     the comparison loops the plain per-subroutine drop-in (mhdgpu_advance,
     path PLAIN) box by box, and the fused single-box step box by box.
   alfven_diag_128: the 128^3 plain drop-in configuration, a linear Alfven wave
@@ -492,7 +493,8 @@ def main():
                   "ic": "per box: linear Alfven wave on the box diagonal or turbulent start "
                         "(k^-2 velocity, k^-3 vector potential), amplitude log-uniform in [1e-4,1e-1]",
                   "cfl": CFL, "cfl_mode": "c_path",
-                  "path": "batched: one persistent launch per sweep over all boxes, one CUDA graph per step",
+                  "path": "batched: per sweep one persistent launch per pencil-length class over all "
+                          "boxes, the classes concurrent, one CUDA graph per step",
                   "l2": "flushed between timed steps (512 MB write, outside the timed events); state 0.87 GB > L2",
                   "parallelism": f"replicas x{args.gpus}"}
     else:

@@ -274,10 +274,14 @@ int mhdgpu_write_check(const char *prefix, const float *u, const float *b, int n
  * one box: Heterogeneous_MHD/C/mhd.c:59-125).  Many independent periodic
  * boxes, each with its own sizes (1 .. MHD_BATCH_MAX_PENCIL cells on every
  * axis; non-cubic and uneven allowed), state, clock and dt, advance together.
- * A step is one CFL launch over all boxes, one clock launch and one persistent
- * launch per sweep (x, y, z, z, y, x), whatever the number of boxes; each box
- * goes through the transpose-free step of mhdgpu_step_fused and ends bit for
- * bit where mhdgpu_advance(path = MHD_PATH_FUSED) takes it alone.
+ * A step is one clock launch and, per sweep (x, y, z, z, y, x), one
+ * persistent launch per pencil-length class present (the boxes whose pencils
+ * along the sweep share a team shape; at most 64 boxes per launch), the
+ * classes of a sweep running concurrently on side streams; the CFL reduction
+ * runs once per mhdgpu_batch_advance call and is otherwise folded into each
+ * step's last sweep.  Each box goes through the transpose-free step of
+ * mhdgpu_step_fused and ends bit for bit where
+ * mhdgpu_advance(path = MHD_PATH_FUSED) takes it alone.
  *
  * The state of box i stays in the caller's device arrays d_u[i] (5 floats
  * per cell) and d_b[i] (3 per cell), reference layout; the handle keeps the
@@ -295,8 +299,8 @@ size_t mhdgpu_batch_workspace_bytes(int nbox, const int *dims /* 3*nbox: nx,ny,n
 int mhdgpu_batch_create(mhdgpu_batch **out, int nbox, const int *dims, float *const *d_u,
                         float *const *d_b, double cfl_number, int cfl_mode, const float *tf);
 int mhdgpu_batch_destroy(mhdgpu_batch *bt);
-/* enqueues nsteps steps on stream (8 launches per step; capturable into a
- * CUDA graph, no host synchronisation) */
+/* enqueues nsteps steps on stream (capturable into a CUDA graph, no host
+ * synchronisation; the side streams fork from and join back to stream) */
 int mhdgpu_batch_advance(mhdgpu_batch *bt, int nsteps, mhdgpu_stream_t stream);
 /* synchronises stream and copies the nbox clocks to the host; returns
  * MHD_ERR_TIMEOUT after a stall, MHD_ERR_UNPHYSICAL when a box's health

@@ -33,18 +33,14 @@ PencilCfg advect_pick(int n)
 template <int CPL, int WPP, class M, bool ROWS, int NT>
 static cudaError_t launch_advect_inst(const AdvectArgs &a, int ppc, cudaStream_t s)
 {
-    static size_t smem_set = 0;
+    static std::atomic<size_t> smem_set[kSmemCacheDevices];
     const int threads = 32 * WPP * ppc;
     const long long blocks = ROWS ? (long long)((a.f.ny + ppc - 1) / ppc) * a.f.nz
                                   : (a.f.npen + ppc - 1) / ppc;
     const size_t smem = sizeof(float) * (size_t)ax_smem_floats(a.f.n, ppc, ROWS);
     if (smem > 227 * 1024) return cudaErrorInvalidConfiguration;
-    if (smem > 48 * 1024 && smem_set < smem) {
-        cudaError_t e = cudaFuncSetAttribute(advect_flux_kernel<CPL, WPP, M, ROWS, NT>,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        smem_set = smem;
-    }
+    const cudaError_t e = ensure_dynamic_smem((const void *)advect_flux_kernel<CPL, WPP, M, ROWS, NT>, smem, smem_set);
+    if (e != cudaSuccess) return e;
     advect_flux_kernel<CPL, WPP, M, ROWS, NT><<<(unsigned)blocks, threads, smem, s>>>(a);
     return cudaGetLastError();
 }

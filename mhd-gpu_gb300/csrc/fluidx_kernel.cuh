@@ -376,18 +376,14 @@ fluidx_kernel(FluidxArgs a)
 template <int CPL, int WPP, class M, bool ROWS, int NT>
 cudaError_t launch_fluidx_inst(const FluidxArgs &a, int ppc, cudaStream_t s)
 {
-    static size_t smem_set = 0;
+    static std::atomic<size_t> smem_set[kSmemCacheDevices];
     const int threads = 32 * WPP * ppc;
     const long long blocks = ROWS ? (long long)((a.f.ny + ppc - 1) / ppc) * a.f.nz
                                   : (a.f.npen + ppc - 1) / ppc;
     const size_t smem = sizeof(float) * (size_t)fx_smem_floats(a.f.n, ppc, WPP, ROWS);
     if (smem > 227 * 1024) return cudaErrorInvalidConfiguration;
-    if (smem > 48 * 1024 && smem_set < smem) {
-        cudaError_t e = cudaFuncSetAttribute(fluidx_kernel<CPL, WPP, M, ROWS, NT>,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        smem_set = smem;
-    }
+    const cudaError_t e = ensure_dynamic_smem((const void *)fluidx_kernel<CPL, WPP, M, ROWS, NT>, smem, smem_set);
+    if (e != cudaSuccess) return e;
     fluidx_kernel<CPL, WPP, M, ROWS, NT><<<(unsigned)blocks, threads, smem, s>>>(a);
     return cudaGetLastError();
 }

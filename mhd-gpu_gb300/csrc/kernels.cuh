@@ -4,6 +4,8 @@
 
 #include <cuda_runtime.h>
 
+#include <atomic>
+
 #include "mhd_common.cuh"
 
 namespace mhd {
@@ -75,5 +77,25 @@ cudaError_t launch_clock(mhdgpu_clock *clk, double cfl_number, float tf, float *
 
 // sets the calling thread's message returned by mhdgpu_last_error()
 void set_last_error(const char *msg);
+
+// Raises a kernel's dynamic shared-memory limit to smem when above the 48 KB
+// default, once per device and size (cache: one word per device ordinal;
+// devices beyond it set the attribute on every call).  Thread-safe.
+constexpr int kSmemCacheDevices = 16;
+inline cudaError_t ensure_dynamic_smem(const void *fn, size_t smem, std::atomic<size_t> *cache)
+{
+    if (smem <= 48 * 1024) return cudaSuccess;
+    int dev = -1;
+    if (cudaGetDevice(&dev) != cudaSuccess) dev = -1;
+    const bool cached = dev >= 0 && dev < kSmemCacheDevices;
+    if (cached && cache[dev].load(std::memory_order_relaxed) >= smem) return cudaSuccess;
+    const cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess && cached) {
+        size_t cur = cache[dev].load(std::memory_order_relaxed);
+        while (cur < smem && !cache[dev].compare_exchange_weak(cur, smem)) {
+        }
+    }
+    return e;
+}
 
 }  // namespace mhd
