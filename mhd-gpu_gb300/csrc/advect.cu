@@ -13,11 +13,11 @@ advect_flux_kernel(AdvectArgs a)
 
 // one thread per stored cell (advect_b1_cell, advect_kernel.cuh)
 __global__ void __launch_bounds__(256)
-advect_b1_kernel(float *b, const float *sA, const float *sB, Frame f, long long ncell)
+advect_b1_kernel(const AdvectArgs a, unsigned ncell)
 {
-    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const unsigned c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= ncell) return;
-    advect_b1_cell(b, sA, sB, f, c);
+    advect_b1_cell(a, c);
 }
 
 PencilCfg advect_pick(int n)
@@ -37,7 +37,7 @@ static cudaError_t launch_advect_inst(const AdvectArgs &a, int ppc, cudaStream_t
     const int threads = 32 * WPP * ppc;
     const long long blocks = ROWS ? (long long)((a.f.ny + ppc - 1) / ppc) * a.f.nz
                                   : (a.f.npen + ppc - 1) / ppc;
-    const size_t smem = sizeof(float) * (size_t)ax_smem_floats(a.f.n, ppc, ROWS);
+    const size_t smem = sizeof(float) * (size_t)ax_tile_smem_floats(NT > 0 ? NT : a.f.n, ppc, CPL, WPP, ROWS);
     if (smem > 227 * 1024) return cudaErrorInvalidConfiguration;
     const cudaError_t e = ensure_dynamic_smem((const void *)advect_flux_kernel<CPL, WPP, M, ROWS, NT>, smem, smem_set);
     if (e != cudaSuccess) return e;
@@ -75,7 +75,7 @@ cudaError_t launch_advect(const AdvectArgs &a, const PencilCfg &cfg, int math, c
     if (e != cudaSuccess) return e;
     const long long ncell = a.f.npen * a.f.n;
     const long long nb = (ncell + 255) / 256;
-    advect_b1_kernel<<<(unsigned)nb, 256, 0, s>>>(a.b, a.sA, a.sB, a.f, ncell);
+    advect_b1_kernel<<<(unsigned)nb, 256, 0, s>>>(a, (unsigned)ncell);
     return cudaGetLastError();
 }
 

@@ -20,6 +20,7 @@
 // fluidx_kernel.cuh.
 #pragma once
 
+#include "advect_reg.cuh"
 #include "kernels.cuh"
 
 namespace mhd {
@@ -41,10 +42,17 @@ __host__ __device__ inline long long ax_smem_floats(int n, int ppc, bool rows)
     if (rows) s += (long long)n * (ax_r2(ppc) + 2 * ax_rk(ppc));
     return s;
 }
+// shared floats of the tile that a (cpl, wpp) team takes for pencils of n
+// cells: register-blocked (advect_reg.cuh) when the pencil fills the team
+__host__ __device__ inline long long ax_tile_smem_floats(int n, int ppc, int cpl, int wpp, bool rows)
+{
+    return reg_tile_shape(n, cpl, wpp) ? axr_smem_floats(n, ppc) : ax_smem_floats(n, ppc, rows);
+}
 
-// One CTA's work on its group of pencils (see fluidx_tile).
+// One CTA's work on its group of pencils (see fluidx_tile_team), any pencil
+// length up to the team's capacity.
 template <int CPL, int WPP, class M, bool ROWS, int NT>
-__device__ __forceinline__ void advect_tile(const AdvectArgs &a, long long tile)
+__device__ __forceinline__ void advect_tile_team(const AdvectArgs &a, long long tile)
 {
     constexpr int TPP = team_threads<WPP>();
     extern __shared__ float smem[];
@@ -274,25 +282,40 @@ __device__ __forceinline__ void advect_tile(const AdvectArgs &a, long long tile)
     }
 }
 
+// One CTA's work on a tile (advect_flux_kernel, the batched kernel): pencils
+// that fill a team of at most one warp exactly take the register-blocked tile
+// (same results).
+template <int CPL, int WPP, class M, bool ROWS, int NT>
+__device__ __forceinline__ void advect_tile(const AdvectArgs &a, long long tile)
+{
+    if constexpr (NT > 0 && reg_tile_shape(NT, CPL, WPP))
+        advect_tile_reg<CPL, team_threads<WPP>(), M, ROWS>(a, tile);
+    else
+        advect_tile_team<CPL, WPP, M, ROWS, NT>(a, tile);
+}
+
 // b(1) = (((b(1) - sA(i,j,k)) + sA(i,j+1,k)) - sB(i,j,k)) + sB(i,j,k+1) for
 // stored cell c; j, k and the neighbours follow the frame's strides.  Plain
 // coherent loads: the batched sweep kernel writes sA, sB earlier in the same
-// launch.  (ncell < 2^31, so the index divisions run in 32 bits.)
-__device__ __forceinline__ void advect_b1_cell(float *b, const float *sA, const float *sB,
-                                               const Frame &f, long long c)
+// launch.  (ncell < 2^31: the index arithmetic runs in 32 bits, the divisions
+// as multiplies, FastDiv.)
+__device__ __forceinline__ void advect_b1_cell(const AdvectArgs &a, unsigned c)
 {
-    const unsigned cu = (unsigned)c;
-    const int j = (int)((cu / (unsigned)f.sj) % (unsigned)f.ny);
-    const int k = (int)((cu / (unsigned)f.sk) % (unsigned)f.nz);
-    const long long cj = c + ((j + 1 == f.ny) ? -(long long)(f.ny - 1) * f.sj : f.sj);
-    const long long ck = c + ((k + 1 == f.nz) ? -(long long)(f.nz - 1) * f.sk : f.sk);
+    const Frame &f = a.f;
+    const unsigned qj = fast_div(c, a.dsj), qk = fast_div(c, a.dsk);
+    const unsigned j = qj - fast_div(qj, a.dny) * (unsigned)f.ny;
+    const unsigned k = qk - fast_div(qk, a.dnz) * (unsigned)f.nz;
+    const unsigned sj = (unsigned)f.sj, sk = (unsigned)f.sk;
+    const unsigned cj = (j + 1 == (unsigned)f.ny) ? c - j * sj : c + sj;
+    const unsigned ck = (k + 1 == (unsigned)f.nz) ? c - k * sk : c + sk;
     const int p1 = nib(f.pb, 0);
-    float bx = b[c * 3 + p1];
-    bx = fsub(bx, sA[c]);
-    bx = fadd(bx, sA[cj]);
-    bx = fsub(bx, sB[c]);
-    bx = fadd(bx, sB[ck]);
-    b[c * 3 + p1] = bx;
+    float *bp = a.b + (size_t)c * 3 + p1;
+    float bx = *bp;
+    bx = fsub(bx, a.sA[c]);
+    bx = fadd(bx, a.sA[cj]);
+    bx = fsub(bx, a.sB[c]);
+    bx = fadd(bx, a.sB[ck]);
+    *bp = bx;
 }
 
 }  // namespace mhd

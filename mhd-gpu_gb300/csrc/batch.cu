@@ -263,8 +263,8 @@ int build_tables(mhdgpu_batch &bt)
                 gr[slot * g.nb + b] = per;
                 acc += items;
                 if (slot == 0) {
-                    sm = std::max(sm, fx_smem_floats(f.n, ppc, tpp / 32, rows));
-                    sm = std::max(sm, ax_smem_floats(f.n, ppc, rows));
+                    sm = std::max(sm, fx_tile_smem_floats(f.n, ppc, batch_class_cpl(g.cls), batch_class_wpp(g.cls), rows));
+                    sm = std::max(sm, ax_tile_smem_floats(f.n, ppc, batch_class_cpl(g.cls), batch_class_wpp(g.cls), rows));
                 }
             }
         }
@@ -284,7 +284,7 @@ int build_tables(mhdgpu_batch &bt)
                 fa.push_back(FluidxArgs{d.u, d.u, d.b, &d.clk->dt, &d.clk->health, f, &d.clk->cmax, bt.cfl_mode});
             else
                 fa.push_back(FluidxArgs{d.u, d.u, d.b, &d.clk->dt, &d.clk->health, f});
-            aa.push_back(AdvectArgs{d.b, d.u, &d.clk->dt, d.scr, d.scr + f.npen * f.n, f});
+            aa.push_back(make_advect_args(d.b, d.u, &d.clk->dt, d.scr, d.scr + f.npen * f.n, f));
         }
     }
     // grids: every group gets the whole GPU at its kernel's occupancy (capped

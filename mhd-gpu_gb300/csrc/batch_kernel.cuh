@@ -67,6 +67,15 @@ __host__ __device__ inline int batch_class_tpp(int c)
     return c == 4 ? 16 : (c == 6 ? 64 : (c == 7 ? 128 : 32));
 }
 __host__ __device__ inline int batch_tpp(int n) { return batch_class_tpp(batch_class(n)); }
+// cells per thread and warps per pencil of a class (MHD_BATCH_CLASSES)
+__host__ __device__ inline int batch_class_cpl(int c)
+{
+    return (c == 2 || c == 4) ? 3 : (c == 0 ? 1 : (c == 3 ? 4 : 2));
+}
+__host__ __device__ inline int batch_class_wpp(int c)
+{
+    return c == 4 ? 0 : (c == 6 ? 2 : (c == 7 ? 4 : 1));
+}
 
 // items of a phase: tiles of ppc pencils (contiguous pencils are numbered
 // linearly, pencils across memory by (j-block, k)), or chunks of cells
@@ -151,9 +160,9 @@ __device__ inline bool batch_wait(const unsigned *ctr, unsigned target, unsigned
 
 __device__ __forceinline__ void batch_b1(const AdvectArgs &a, long long c0, int cells)
 {
-    const long long ncell = a.f.npen * a.f.n;
-    const long long c1 = min(c0 + cells, ncell);
-    for (long long c = c0 + threadIdx.x; c < c1; c += blockDim.x) advect_b1_cell(a.b, a.sA, a.sB, a.f, c);
+    const unsigned ncell = (unsigned)(a.f.npen * a.f.n);
+    const unsigned c1 = min((unsigned)c0 + (unsigned)cells, ncell);
+    for (unsigned c = (unsigned)c0 + threadIdx.x; c < c1; c += blockDim.x) advect_b1_cell(a, c);
 }
 
 // One sweep of the boxes of one class.  At most 256 threads per CTA; MINB

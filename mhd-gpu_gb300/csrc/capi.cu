@@ -108,7 +108,7 @@ int mhdgpu_advectbyzx(float *b, const float *u, int nx, int ny, int nz, const fl
     if (st) return st;
     if (!b || !u || !d_dt || !d_scratch) return fail(MHD_ERR_ARG, "mhdgpu_advectbyzx: null pointer");
     const long long ncell = (long long)nx * ny * nz;
-    AdvectArgs a{b, u, d_dt, d_scratch, d_scratch + ncell, make_frame(nx, ny, nz)};
+    AdvectArgs a = make_advect_args(b, u, d_dt, d_scratch, d_scratch + ncell, make_frame(nx, ny, nz));
     ProfScope ps(MHD_KCLASS_ADVECT, 2, (cudaStream_t)stream);
     MHD_CU(launch_advect(a, pencil_cfg(MHD_KCLASS_ADVECT, nx), math_mode(), (cudaStream_t)stream), "mhdgpu_advectbyzx");
     return MHD_OK;
@@ -261,7 +261,7 @@ static int sweep_view(float *u, float *b, const Frame &f, const float *dt, float
 {
     const long long ncell = f.npen * f.n;
     FluidxArgs fa{u, u, b, dt, health, f, cfl, cfl_mode};
-    AdvectArgs aa{b, u, dt, scr, scr + ncell, f};
+    AdvectArgs aa = make_advect_args(b, u, dt, scr, scr + ncell, f);
     for (int part = 0; part < 2; ++part) {
         if ((part == 0) == fluid_first) {
             ProfScope ps(MHD_KCLASS_FLUIDX, 1, s);

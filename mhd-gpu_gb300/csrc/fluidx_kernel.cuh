@@ -26,6 +26,7 @@
 // issue.
 #pragma once
 
+#include "fluidx_reg.cuh"
 #include "kernels.cuh"
 
 namespace mhd {
@@ -51,12 +52,19 @@ __host__ __device__ inline long long fx_smem_floats(int n, int ppc, int wpp, boo
 {
     return (long long)ppc * fx_ps(n, rows) + fx_xsize(n, ppc, rows) + (long long)ppc * wpp;
 }
+// shared floats of the tile that a (cpl, wpp) team takes for pencils of n
+// cells: register-blocked (fluidx_reg.cuh) when the pencil fills the team
+__host__ __device__ inline long long fx_tile_smem_floats(int n, int ppc, int cpl, int wpp, bool rows)
+{
+    return reg_tile_shape(n, cpl, wpp) ? fxr_smem_floats(n, ppc, rows) : fx_smem_floats(n, ppc, wpp, rows);
+}
 
 // One CTA's work: tile = the CTA's group of pencils (contiguous mode: pencils
-// tile*ppc ..; rows mode: j-block tile % njb of plane tile / njb).  Called once
-// per CTA by fluidx_kernel and in a loop by the batched kernel (batch.cu).
+// tile*ppc ..; rows mode: j-block tile % njb of plane tile / njb), for any
+// pencil length up to the team's capacity.  fluidx_tile below picks it or the
+// register-blocked tile.
 template <int CPL, int WPP, class M, bool ROWS, int NT>
-__device__ __forceinline__ void fluidx_tile(const FluidxArgs &a, long long tile)
+__device__ __forceinline__ void fluidx_tile_team(const FluidxArgs &a, long long tile)
 {
     constexpr int TPP = team_threads<WPP>();
     extern __shared__ float smem[];
@@ -364,6 +372,18 @@ __device__ __forceinline__ void fluidx_tile(const FluidxArgs &a, long long tile)
     }
 }
 
+// One CTA's work on a tile; called once per CTA by fluidx_kernel and in a loop
+// by the batched kernel (batch_kernel.cuh).  Pencils that fill a team of at
+// most one warp exactly take the register-blocked tile (same results).
+template <int CPL, int WPP, class M, bool ROWS, int NT>
+__device__ __forceinline__ void fluidx_tile(const FluidxArgs &a, long long tile)
+{
+    if constexpr (NT > 0 && reg_tile_shape(NT, CPL, WPP))
+        fluidx_tile_reg<CPL, team_threads<WPP>(), M, ROWS>(a, tile);
+    else
+        fluidx_tile_team<CPL, WPP, M, ROWS, NT>(a, tile);
+}
+
 template <int CPL, int WPP, class M, bool ROWS, int NT>
 __global__ void __launch_bounds__(256)
 fluidx_kernel(FluidxArgs a)
@@ -380,7 +400,7 @@ cudaError_t launch_fluidx_inst(const FluidxArgs &a, int ppc, cudaStream_t s)
     const int threads = 32 * WPP * ppc;
     const long long blocks = ROWS ? (long long)((a.f.ny + ppc - 1) / ppc) * a.f.nz
                                   : (a.f.npen + ppc - 1) / ppc;
-    const size_t smem = sizeof(float) * (size_t)fx_smem_floats(a.f.n, ppc, WPP, ROWS);
+    const size_t smem = sizeof(float) * (size_t)fx_tile_smem_floats(NT > 0 ? NT : a.f.n, ppc, CPL, WPP, ROWS);
     if (smem > 227 * 1024) return cudaErrorInvalidConfiguration;
     const cudaError_t e = ensure_dynamic_smem((const void *)fluidx_kernel<CPL, WPP, M, ROWS, NT>, smem, smem_set);
     if (e != cudaSuccess) return e;

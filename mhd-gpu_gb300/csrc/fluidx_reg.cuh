@@ -1,0 +1,434 @@
+// fluidx_reg.cuh - the fluid sweep, register-blocked, for pencils whose length
+// fills a team of at most one warp exactly (n = 32*CPL, or 16*CPL for
+// half-warp teams): the 32, 48, 64, 96 and 128-cell pencils.
+//
+// Algorithm and rounding: exactly fluidx_tile's (fluidx_kernel.cuh; reference
+// Heterogeneous_MHD/C/fluidx.c:19-102, tvd1.c:8-118, mhdflux.c:9-72),
+// operation for operation, so the two give the same bits.  Only the data
+// movement differs:
+//  - thread t of a team owns the consecutive cells t*CPL .. t*CPL+CPL-1, so a
+//    stencil neighbour (i-1, i+1, i+2) is in the thread's own registers or, at
+//    the ends of its run, in the adjacent lane's, fetched with a warp shuffle;
+//    lane 0's left neighbour is lane TPP-1, which is the pencil's periodic
+//    wrap;
+//  - each difference of the limiter is formed once and used by both cells
+//    that need it, and fl = c*wl once per cell;
+//  - u is staged component-major per pencil ([pencil][component][cell], rows
+//    of n+4 floats), so a thread reads or writes one component of its run with
+//    one vector access; b stays cell-major;
+//  - there are no exchange rows in shared memory and no team barriers.
+#pragma once
+
+#include "kernels.cuh"
+
+namespace mhd {
+
+// shared-memory geometry (floats); every offset is a multiple of 4 floats
+__host__ __device__ inline int fxr_cs(int n) { return n + 4; }                    // a component of u
+__host__ __device__ inline int fxr_ps(int n) { return 5 * fxr_cs(n); }            // u of one pencil
+__host__ __device__ inline int fxr_bs(int n, bool rows) { return rows ? 3 * n + 4 : 3 * n; }   // b of one pencil
+__host__ __device__ inline int fxr_ks(int n) { return n + 4; }                    // rows: b(3) of the k+1 pencil
+__host__ __device__ inline long long fxr_smem_floats(int n, int ppc, bool rows)
+{
+    long long s = (long long)ppc * fxr_ps(n);
+    if (rows) s += (long long)(ppc + 1) * fxr_bs(n, true) + (long long)ppc * fxr_ks(n);
+    else s += (long long)ppc * fxr_bs(n, false);
+    return s;
+}
+
+// the lanes of one team (TPP = 16 or 32 consecutive lanes of a warp)
+template <int TPP>
+struct Lanes {
+    int t;   // lane within the team
+    // v of lane t+d of the team, periodic.  Every lane of the warp calls it.
+    __device__ __forceinline__ float from(float v, int d) const
+    {
+        return __shfl_sync(0xffffffffu, v, (t + d + TPP) & (TPP - 1), TPP);
+    }
+    // max over the team (values >= 0; NaN dropped as Team::pencil_max drops it)
+    __device__ __forceinline__ float max(float x) const
+    {
+#pragma unroll
+        for (int o = TPP / 2; o > 0; o >>= 1) x = fmaxf(x, __shfl_xor_sync(0xffffffffu, x, o));
+        return x;
+    }
+};
+
+// K consecutive floats at p in shared memory: 16-byte accesses for K % 4 == 0,
+// 8-byte for K % 2 == 0 (p is aligned accordingly by the geometry above)
+template <int K>
+__device__ __forceinline__ void lds_run(const float *p, float (&v)[K])
+{
+    if constexpr (K % 4 == 0) {
+#pragma unroll
+        for (int i = 0; i < K / 4; ++i) {
+            const float4 x = reinterpret_cast<const float4 *>(p)[i];
+            v[4 * i] = x.x; v[4 * i + 1] = x.y; v[4 * i + 2] = x.z; v[4 * i + 3] = x.w;
+        }
+    } else if constexpr (K % 2 == 0) {
+#pragma unroll
+        for (int i = 0; i < K / 2; ++i) {
+            const float2 x = reinterpret_cast<const float2 *>(p)[i];
+            v[2 * i] = x.x; v[2 * i + 1] = x.y;
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < K; ++i) v[i] = p[i];
+    }
+}
+
+template <int K>
+__device__ __forceinline__ void sts_run(float *p, const float (&v)[K])
+{
+    if constexpr (K % 4 == 0) {
+#pragma unroll
+        for (int i = 0; i < K / 4; ++i)
+            reinterpret_cast<float4 *>(p)[i] = make_float4(v[4 * i], v[4 * i + 1], v[4 * i + 2], v[4 * i + 3]);
+    } else if constexpr (K % 2 == 0) {
+#pragma unroll
+        for (int i = 0; i < K / 2; ++i) reinterpret_cast<float2 *>(p)[i] = make_float2(v[2 * i], v[2 * i + 1]);
+    } else {
+#pragma unroll
+        for (int i = 0; i < K; ++i) p[i] = v[i];
+    }
+}
+
+// component ii of the thread's run of u, or of the default state
+// (1, 0, 0, 0, 1) for a pencil that is not live (it computes on harmless
+// values and stores nothing)
+template <int CPL>
+__device__ __forceinline__ void load_comp(const float *p, bool live, int ii, float (&v)[CPL])
+{
+    if (live) {
+        lds_run<CPL>(p, v);
+    } else {
+#pragma unroll
+        for (int m = 0; m < CPL; ++m) v[m] = (ii == 0 || ii == 4) ? 1.0f : 0.0f;
+    }
+}
+
+template <int CPL, int TPP, class M, bool ROWS>
+__device__ __forceinline__ void fluidx_tile_reg(const FluidxArgs &a, long long tile)
+{
+    constexpr int N = TPP * CPL;
+    constexpr int CS = N + 4, PS = 5 * CS, BSC = 3 * N, BSR = 3 * N + 4, KS = N + 4;
+    extern __shared__ __align__(16) float smem_r[];
+    float *smem = smem_r;
+    const Frame &f = a.f;
+    const int ppc = blockDim.x / TPP;
+    const int q = threadIdx.x / TPP;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    const Lanes<TPP> ln{(int)(threadIdx.x & (TPP - 1))};
+    const int c0 = ln.t * CPL;
+
+    long long p0 = 0;          // !ROWS: first linear pencil
+    int j0 = 0, k = 0;         // ROWS: first j and the plane
+    int nvalid;
+    if (!ROWS) {
+        p0 = tile * ppc;
+        nvalid = (int)min((long long)ppc, f.npen - p0);
+    } else {
+        const int njb = (f.ny + ppc - 1) / ppc;
+        k = (int)(tile / njb);
+        j0 = (int)(tile - (long long)k * njb) * ppc;
+        nvalid = min(ppc, f.ny - j0);
+    }
+    const bool live = q < nvalid;
+    const int jq = ROWS ? j0 + q : (live ? (int)((p0 + q) % f.ny) : 0);
+    const int kq = ROWS ? k : (live ? (int)((p0 + q) / f.ny) : 0);
+
+    float *US = smem;                       // ppc * PS, component-major
+    float *us = US + q * PS + c0;           // component ii of the run: us + ii*CS
+    float *BS = smem + ppc * PS;            // b staging
+    const float dt = *a.dt;
+
+    // ---- stage u (kept) and b; cell-centred B of the run ----
+    float bc[CPL][3];
+    const float *bjp = nullptr, *bkp = nullptr;   // !ROWS: b of the j+1 and k+1 pencils
+    {
+        float bo[3 * CPL], bj[CPL], bk[CPL];   // own b; b(2) at j+1; b(3) at k+1
+        if (!ROWS) {
+            const float *gu = a.u_in + p0 * 5 * N;
+            const int cells = nvalid * N;
+            for (int c = threadIdx.x; c < cells; c += blockDim.x) {
+                const int qq = c / N, cc = c - qq * N;
+                float *d = US + qq * PS + cc;
+                const float *s = gu + (long long)c * 5;
+#pragma unroll
+                for (int ii = 0; ii < 5; ++ii) cp_async4(d + ii * CS, s + ii);
+            }
+            // b as it lies; completes this thread's u copies too
+            block_copy_in(BS, a.b + p0 * 3 * N, (long long)nvalid * 3 * N, threadIdx.x, blockDim.x);
+            __syncthreads();
+            const int jp = (jq + 1 == f.ny) ? 0 : jq + 1;
+            const int kp = (kq + 1 == f.nz) ? 0 : kq + 1;
+            bjp = a.b + ((long long)kq * f.ny + jp) * 3 * N;
+            bkp = a.b + ((long long)kp * f.ny + jq) * 3 * N;
+            if (live) {
+                lds_run<3 * CPL>(BS + q * BSC + c0 * 3, bo);
+#pragma unroll
+                for (int m = 0; m < CPL; ++m) {
+                    bj[m] = bjp[(c0 + m) * 3 + 1];
+                    bk[m] = bkp[(c0 + m) * 3 + 2];
+                }
+            }
+        } else {
+            const long long kb = (long long)k * f.sk;
+            const int kp = (k + 1 == f.nz) ? 0 : k + 1;
+            const long long kpb = (long long)kp * f.sk;
+            float *SB = BS;                          // (ppc+1) * BSR: b of columns j0 .. j0+nvalid
+            float *SK = BS + (ppc + 1) * BSR;        // ppc * KS: b(3) of plane k+1, [pencil][i]
+            const int ru = 5 * nvalid, rb = 3 * (nvalid + 1);
+            const int pb2 = nib(f.pb, 2);
+            // per-lane offsets, independent of the row: a row of u is ru floats
+            // at u_in + (rowc + j0)*5, element r -> pencil r/5, stored component r%5
+            int us_off[2], sb_off[2], gb_off[2];
+            bool us_on[2], sb_on[2];
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int r = lane + 32 * h;
+                us_on[h] = r < ru;
+                const int qq = r / 5, p = r - qq * 5;
+                us_off[h] = qq * PS + nib(f.iu, p) * CS;
+                sb_on[h] = r < rb;
+                const int qb = r / 3, pp = r - qb * 3;
+                int j = j0 + qb;
+                if (j >= f.ny) j -= f.ny;
+                sb_off[h] = qb * BSR + nib(f.ib, pp);
+                gb_off[h] = j * 3 + pp;
+            }
+            const bool sk_on = lane < nvalid;
+            for (int i = warp; i < N; i += nwarps) {
+                const long long rowc = kb + (long long)i * f.si;    // cell of (i, 0, k)
+                const float *gu = a.u_in + (rowc + j0) * 5;
+                const float *gb = a.b + rowc * 3;
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    if (us_on[h]) cp_async4(&US[us_off[h] + i], gu + lane + 32 * h);
+                    if (sb_on[h]) cp_async4(&SB[sb_off[h] + i * 3], gb + gb_off[h]);
+                }
+                if (sk_on)
+                    cp_async4(&SK[lane * KS + i], a.b + (kpb + (long long)i * f.si + j0 + lane) * 3 + pb2);
+            }
+            cp_async_wait_all();
+            __syncthreads();
+            if (live) {
+                float bn[3 * CPL];
+                lds_run<3 * CPL>(SB + q * BSR + c0 * 3, bo);
+                lds_run<3 * CPL>(SB + (q + 1) * BSR + c0 * 3, bn);
+#pragma unroll
+                for (int m = 0; m < CPL; ++m) bj[m] = bn[m * 3 + 1];
+                lds_run<CPL>(SK + q * KS + c0, bk);
+            }
+        }
+        if (!live) {
+#pragma unroll
+            for (int m = 0; m < CPL; ++m) {
+                bo[3 * m] = 0.0f; bo[3 * m + 1] = 0.0f; bo[3 * m + 2] = 0.0f;
+                bj[m] = 0.0f; bk[m] = 0.0f;
+            }
+        }
+        // b3x = b/2 ; b3x(1) += cshift(b3x(1),1) ; b3x(2) += b(2,jp)/2 ;
+        // b3x(3) += b(3,kp)/2   (fluidx.c:71-81; the halvings are exact)
+        const float nb0 = ln.from(bo[0], 1);   // b(1) of the cell after the run
+#pragma unroll
+        for (int m = 0; m < CPL; ++m) {
+            const float bnext = (m + 1 < CPL) ? bo[3 * (m + 1)] : nb0;
+            bc[m][0] = fadd(0.5f * bo[3 * m], 0.5f * bnext);
+            bc[m][1] = fadd(0.5f * bo[3 * m + 1], 0.5f * bj[m]);
+            bc[m][2] = fadd(0.5f * bo[3 * m + 2], 0.5f * bk[m]);
+        }
+    }
+
+    const float hdt = 0.5f * dt;
+    unsigned bad = 0;
+    float u1[CPL][5];
+
+    // ================= half step =================
+    {
+        float v[CPL][5];
+        float cl = 0.0f;
+        {
+            float uc[5][CPL];
+#pragma unroll
+            for (int ii = 0; ii < 5; ++ii) load_comp<CPL>(us + ii * CS, live, ii, uc[ii]);
+#pragma unroll
+            for (int m = 0; m < CPL; ++m) {
+                const float uu[5] = {uc[0][m], uc[1][m], uc[2][m], uc[3][m], uc[4][m]};
+                float cs, p;
+                cell_flux<M>(uu, bc[m], v[m], cs, p);
+                cl = fmaxf(cl, cs);
+            }
+        }
+        const float c = ln.max(cl);
+        const bool cpos = c > 0.0f;
+        const float yc = cpos ? M::recip(c) : 0.0f;
+#pragma unroll
+        for (int ii = 0; ii < 5; ++ii) {
+            float uu[CPL], wl[CPL], fl[CPL];
+            load_comp<CPL>(us + ii * CS, live, ii, uu);
+            // fr = c(u + v/c) (kept in u1), wl = u - v/c
+#pragma unroll
+            for (int m = 0; m < CPL; ++m) {
+                const float vv = cpos ? M::divy(v[m][ii], c, yc) : v[m][ii];
+                u1[m][ii] = M::mul(c, M::add(uu[m], vv));
+                wl[m] = M::sub(uu[m], vv);
+            }
+            // flux = (fr - c*cshift(wl,+1))/2
+            const float wr = ln.from(wl[0], 1);
+#pragma unroll
+            for (int m = 0; m < CPL; ++m)
+                fl[m] = 0.5f * M::sub(u1[m][ii], M::mul(c, (m + 1 < CPL) ? wl[m + 1] : wr));
+            // u1 = u - (flux - cshift(flux,-1)) dt/2
+            const float fm = ln.from(fl[CPL - 1], -1);
+#pragma unroll
+            for (int m = 0; m < CPL; ++m)
+                u1[m][ii] = M::add(uu[m], M::mul(-hdt, M::sub(fl[m], m > 0 ? fl[m - 1] : fm)));
+        }
+    }
+
+    // ================= full step =================
+    {
+        float v[CPL][5];
+        float cl = 0.0f;
+#pragma unroll
+        for (int m = 0; m < CPL; ++m) {
+            float cs, p;
+            cell_flux<M>(u1[m], bc[m], v[m], cs, p);
+            cl = fmaxf(cl, cs);
+            if (!(p > 0.0f)) bad |= MHD_HEALTH_PRESSURE;
+        }
+        const float c = ln.max(cl);
+        const bool cpos = c > 0.0f;
+        const float yc = cpos ? M::recip(c) : 0.0f;
+        const float mdt = -dt;
+        float ssum[CPL];
+#pragma unroll
+        for (int m = 0; m < CPL; ++m) ssum[m] = 0.0f;
+#pragma unroll
+        for (int ii = 0; ii < 5; ++ii) {
+            // fr = c(u1 + v/c), fl = c wl = c(u1 - v/c) of the run
+            float fr[CPL], fl[CPL];
+#pragma unroll
+            for (int m = 0; m < CPL; ++m) {
+                const float vv = cpos ? M::divy(v[m][ii], c, yc) : v[m][ii];
+                fr[m] = M::mul(c, M::add(u1[m][ii], vv));
+                fl[m] = M::mul(c, M::sub(u1[m][ii], vv));
+            }
+            // neighbours: fr of cells c0-1 and c0+CPL, fl of c0+CPL and c0+CPL+1
+            const float frl = ln.from(fr[CPL - 1], -1);
+            const float frr = ln.from(fr[0], 1);
+            const float flr1 = ln.from(fl[0], 1);
+            const float flr2 = (CPL >= 2) ? ln.from(fl[CPL >= 2 ? 1 : 0], 1) : ln.from(fl[0], 2);
+            // dr[i] = fr(c0+i) - fr(c0+i-1), dl[i] = fl(c0+i) - fl(c0+i+1), i = 0 .. CPL
+            float dr[CPL + 1], dl[CPL + 1];
+#pragma unroll
+            for (int i = 0; i <= CPL; ++i) {
+                const float ra = (i < CPL) ? fr[i] : frr;
+                const float rb = (i > 0) ? fr[i - 1] : frl;
+                dr[i] = M::sub(ra, rb);
+                const float la = (i < CPL) ? fl[i] : flr1;
+                const float lb = (i + 1 < CPL) ? fl[i + 1] : (i + 1 == CPL ? flr1 : flr2);
+                dl[i] = M::sub(la, lb);
+            }
+            // flux = (fr - fl + dfr - dfl)/2 with van Leer slopes (tvd1.c:54-112):
+            // dfr = slope(fr(c+1)-fr(c), fr(c)-fr(c-1)),
+            // dfl = slope(fl(c+1)-fl(c+2), fl(c)-fl(c+1)), fl0 = fl(c+1)
+            float fx[CPL];
+#pragma unroll
+            for (int m = 0; m < CPL; ++m) {
+                const float dfr = M::slope(dr[m + 1], dr[m]);
+                const float dfl = M::slope(dl[m + 1], dl[m]);
+                const float fl0 = (m + 1 < CPL) ? fl[m + 1] : flr1;
+                fx[m] = 0.5f * M::add(M::sub(fr[m], fl0), M::sub(dfr, dfl));
+            }
+            // u = u - (flux - cshift(flux,-1)) dt, written back into US
+            const float fxl = ln.from(fx[CPL - 1], -1);
+            float uu[CPL], un[CPL];
+            load_comp<CPL>(us + ii * CS, live, ii, uu);
+#pragma unroll
+            for (int m = 0; m < CPL; ++m) {
+                un[m] = M::add(uu[m], M::mul(mdt, M::sub(fx[m], m > 0 ? fx[m - 1] : fxl)));
+                ssum[m] += un[m];
+                if (ii == 0 && !(un[m] > 0.0f)) bad |= MHD_HEALTH_DENSITY;
+            }
+            if (live) sts_run<CPL>(us + ii * CS, un);
+        }
+#pragma unroll
+        for (int m = 0; m < CPL; ++m)
+            if (!isfinite(ssum[m])) bad |= MHD_HEALTH_NONFINITE;
+        // the last x sweep of a step: the CFL fast speed of the updated cells,
+        // as cfl_cell_speed forms it
+        if (!ROWS && a.cfl != nullptr) {
+            const float *bs = BS + q * BSC + c0 * 3;   // this run's staged b
+            const float nb0 = ln.from(live ? bs[0] : 0.0f, 1);
+            float cfl_c = 0.0f;
+            if (live) {
+#pragma unroll
+                for (int m = 0; m < CPL; ++m) {
+                    float um[5], bb[3];
+#pragma unroll
+                    for (int ii = 0; ii < 5; ++ii) um[ii] = us[ii * CS + m];
+                    if (a.cfl_mode == MHD_CFL_C) {
+                        bb[0] = bs[3 * m]; bb[1] = bs[3 * m + 1]; bb[2] = bs[3 * m + 2];
+                        cfl_c = fmaxf(cfl_c, cfl_speed_c(um, bb));
+                    } else {
+                        const float bnext = (m + 1 < CPL) ? bs[3 * (m + 1)] : nb0;
+                        bb[0] = fdiv(fadd(bs[3 * m], bnext), 2.0f);
+                        bb[1] = fdiv(fadd(bs[3 * m + 1], bjp[(c0 + m) * 3 + 1]), 2.0f);
+                        bb[2] = fdiv(fadd(bs[3 * m + 2], bkp[(c0 + m) * 3 + 2]), 2.0f);
+                        cfl_c = fmaxf(cfl_c, cfl_speed_averaged(um, bb));
+                    }
+                }
+            }
+            cfl_block_max(cfl_c, a.cfl);   // every thread of the CTA (a.cfl is uniform)
+        }
+    }
+
+    if (!live) bad = 0;
+    if (bad) flag_health(a.health, bad);
+    __syncthreads();
+    // ---- write back: component-major shared rows -> the cell-major state ----
+    if (!ROWS) {
+        float *g = a.u_out + p0 * 5 * N;
+        const int nf = nvalid * 5 * N;   // a multiple of 4 (N is a multiple of 16)
+        if ((reinterpret_cast<uintptr_t>(g) & 15u) == 0) {
+            for (int e4 = threadIdx.x; e4 < nf / 4; e4 += blockDim.x) {
+                int cell = (4 * e4) / 5, comp = 4 * e4 - 5 * cell;
+                float x[4];
+#pragma unroll
+                for (int r = 0; r < 4; ++r) {
+                    const int qq = cell / N, cc = cell - qq * N;
+                    x[r] = US[qq * PS + comp * CS + cc];
+                    if (++comp == 5) { comp = 0; ++cell; }
+                }
+                reinterpret_cast<float4 *>(g)[e4] = make_float4(x[0], x[1], x[2], x[3]);
+            }
+        } else {
+            for (int e = threadIdx.x; e < nf; e += blockDim.x) {
+                const int cell = e / 5, comp = e - 5 * cell, qq = cell / N, cc = cell - qq * N;
+                g[e] = US[qq * PS + comp * CS + cc];
+            }
+        }
+    } else {
+        const long long kb = (long long)k * f.sk;
+        const int ru = 5 * nvalid;
+        int off[2];
+        bool on[2];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int r = lane + 32 * h;
+            on[h] = r < ru;
+            const int qq = r / 5, p = r - qq * 5;
+            off[h] = qq * PS + nib(f.iu, p) * CS;
+        }
+        for (int i = warp; i < N; i += nwarps) {
+            float *g = a.u_out + (kb + (long long)i * f.si + j0) * 5;
+#pragma unroll
+            for (int h = 0; h < 2; ++h)
+                if (on[h]) g[lane + 32 * h] = US[off[h] + i];
+        }
+    }
+}
+
+}  // namespace mhd

@@ -32,7 +32,22 @@ struct AdvectArgs {
     float *sA;            // ncell: shifted stage-A flux
     float *sB;            // ncell: shifted stage-B flux
     Frame f;
+    // the gather's index arithmetic: stored cell c -> frame j = (c / sj) % ny,
+    // k = (c / sk) % nz, as multiplies (set by make_advect_args)
+    FastDiv dsj, dny, dsk, dnz;
 };
+
+inline AdvectArgs make_advect_args(float *b, const float *u, const float *dt, float *sA, float *sB,
+                                   const Frame &f)
+{
+    AdvectArgs a;
+    a.b = b; a.u = u; a.dt = dt; a.sA = sA; a.sB = sB; a.f = f;
+    a.dsj = make_fastdiv((unsigned)f.sj);
+    a.dny = make_fastdiv((unsigned)f.ny);
+    a.dsk = make_fastdiv((unsigned)f.sk);
+    a.dnz = make_fastdiv((unsigned)f.nz);
+    return a;
+}
 
 // team shape of the pencil kernels: CPL cells per thread, WPP warps per
 // pencil, PPC pencils per CTA

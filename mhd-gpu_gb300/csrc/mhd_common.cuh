@@ -73,6 +73,41 @@ __host__ __device__ inline bool frame_rows(const Frame &f)
 // threads of a pencil team: WPP warps, or half a warp for WPP = 0
 template <int WPP>
 __host__ __device__ constexpr int team_threads() { return WPP == 0 ? 16 : 32 * WPP; }
+__host__ __device__ constexpr int team_threads_of(int wpp) { return wpp == 0 ? 16 : 32 * wpp; }
+
+// A pencil whose length fills a team of at most one warp exactly takes the
+// register-blocked tiles (fluidx_reg.cuh, advect_reg.cuh): thread t owns the
+// consecutive cells t*CPL .. t*CPL+CPL-1 and stencil neighbours come from the
+// adjacent lanes by warp shuffle.  Host and device agree through this test.
+__host__ __device__ constexpr bool reg_tile_shape(int n, int cpl, int wpp)
+{
+    return wpp <= 1 && n == team_threads_of(wpp) * cpl;
+}
+
+// Unsigned division of a cell index n < 2^31 by a fixed divisor d >= 1 as a
+// multiply and a shift: with l = ceil(log2 d), s = 31 + l and m = ceil(2^s / d)
+// (< 2^32), floor(n m / 2^s) = floor(n / d) for every n < 2^31, since
+// m/2^s - 1/d < 2^-(31+l) and so n m / 2^s < n/d + 1/d (Granlund and
+// Montgomery, "Division by invariant integers using multiplication", PLDI
+// 1994, section 4).
+struct FastDiv {
+    unsigned m;
+    int s;
+};
+inline FastDiv make_fastdiv(unsigned d)
+{
+    int l = 0;
+    while ((1ull << l) < d) ++l;
+    const unsigned long long p = 1ull << (31 + l);
+    FastDiv f;
+    f.m = (unsigned)((p + d - 1) / d);
+    f.s = 31 + l;
+    return f;
+}
+__host__ __device__ __forceinline__ unsigned fast_div(unsigned n, FastDiv d)
+{
+    return (unsigned)(((unsigned long long)n * d.m) >> d.s);
+}
 
 // A team of TPP = 32*WPP threads (16 for WPP = 0: two teams share a warp)
 // owns one pencil; thread t holds the CPL

@@ -87,7 +87,7 @@ int mhdgpu_advectbyzx_noalloc(float *b, const float *u, int nx, int ny, int nz, 
     float *scr = nullptr;
     int st = scratch_on_current_device(&scr);
     if (st != MHD_OK) return st;
-    mhd::AdvectArgs a{b, u, d_dt, scr, scr + ncell, mhd::make_frame(nx, ny, nz)};
+    mhd::AdvectArgs a = mhd::make_advect_args(b, u, d_dt, scr, scr + ncell, mhd::make_frame(nx, ny, nz));
     cudaError_t e = mhd::launch_advect(a, mhd::pencil_cfg(MHD_KCLASS_ADVECT, nx), mhd::math_mode(), (cudaStream_t)stream);
     if (e != cudaSuccess) return noalloc_cuda_fail("launch", e);
     return MHD_OK;

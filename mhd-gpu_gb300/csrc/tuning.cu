@@ -185,7 +185,7 @@ int mhdgpu_autotune(int nx, int ny, int nz, int math)
                             FluidxArgs a{u2, u, b, dt, nullptr, f};
                             le = launch_fluidx(a, c, math, s);
                         } else {
-                            AdvectArgs a{b, u, dt, scr, scr + ncell, f};
+                            AdvectArgs a = make_advect_args(b, u, dt, scr, scr + ncell, f);
                             le = launch_advect(a, c, math, s);
                         }
                         if (le != cudaSuccess) { cudaGetLastError(); break; }   // shape not launchable here
