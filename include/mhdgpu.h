@@ -168,7 +168,8 @@ typedef struct {
     float t;        /* simulation time */
     float dt;       /* dt of the last step */
     float inv_c;    /* 1/c_max of the last CFL evaluation */
-    unsigned cmax;  /* CFL reduction word (kept at 0 between steps) */
+    unsigned cmax;  /* CFL reduction word: between steps, the fast speed of the
+                       current state folded in by the last sweep (float bits) */
     unsigned health;/* MHD_HEALTH_* bits */
     int iter;       /* steps taken */
 } mhdgpu_clock;
@@ -179,7 +180,16 @@ typedef struct {
  * entries.  Steps with tf > 0 and t >= tf are skipped on the device (the
  * reference's do-while exit).  path = MHD_PATH_PLAIN (d_work of
  * mhdgpu_step_workspace_bytes) or MHD_PATH_FUSED (of
- * mhdgpu_step_fused_workspace_bytes). */
+ * mhdgpu_step_fused_workspace_bytes).
+ *
+ * The CFL reduction runs as its own pass over the state before the call's
+ * first step; each step's last fluid sweep folds the next step's reduction
+ * into the clock's CFL word, so later steps of the call need no pass.  With
+ * MHD_ADVANCE_RESUME or'ed into cfl_mode, the first step takes that folded
+ * word too: valid only when the clock's last step was taken by mhdgpu_advance
+ * on this same state and the state is unchanged since (a run driven one step
+ * per call, e.g. one step per CUDA graph launch). */
+#define MHD_ADVANCE_RESUME 0x100
 int mhdgpu_advance(float *u, float *b, int nx, int ny, int nz, int nsteps,
                    double cfl_number, int cfl_mode, float tf,
                    mhdgpu_clock *d_clock, float *d_dt_log, void *d_work,
@@ -302,6 +312,12 @@ int mhdgpu_batch_destroy(mhdgpu_batch *bt);
 /* enqueues nsteps steps on stream (capturable into a CUDA graph, no host
  * synchronisation; the side streams fork from and join back to stream) */
 int mhdgpu_batch_advance(mhdgpu_batch *bt, int nsteps, mhdgpu_stream_t stream);
+/* as mhdgpu_batch_advance, continuing the handle's previous advance: the first
+ * step takes the CFL speeds folded into the previous step's last sweep instead
+ * of a reduction pass.  Valid only when no box's state changed since the
+ * handle's last advance; the handle runs the pass anyway when it has not
+ * advanced yet (or its schedule was tuned since). */
+int mhdgpu_batch_resume(mhdgpu_batch *bt, int nsteps, mhdgpu_stream_t stream);
 /* synchronises stream and copies the nbox clocks to the host; returns
  * MHD_ERR_TIMEOUT after a stall, MHD_ERR_UNPHYSICAL when a box's health
  * reports NaN/Inf or rho <= 0 */

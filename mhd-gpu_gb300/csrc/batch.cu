@@ -107,6 +107,7 @@ struct mhdgpu_batch {
     int threads[3] = {256, 256, 256};
     int cps[3] = {8, 8, 8};             // CTAs per SM cap (the occupancy limits it further)
     unsigned stall_extra = 0;           // mhdgpu_batch_inject_stall
+    bool folded = false;                // a step was enqueued: the clocks hold the folded CFL speeds
     ClassWork work{};                   // parameter block of one launch (filled per launch)
     cudaStream_t side[kBatchClasses] = {};
     cudaEvent_t fork = nullptr, join[kBatchClasses] = {};
@@ -469,15 +470,26 @@ int mhdgpu_batch_destroy(mhdgpu_batch *bt)
     return MHD_OK;
 }
 
-int mhdgpu_batch_advance(mhdgpu_batch *bt, int nsteps, mhdgpu_stream_t stream)
+static int batch_steps(mhdgpu_batch *bt, int nsteps, bool resume, mhdgpu_stream_t stream)
 {
-    if (!bt) return bfail(MHD_ERR_ARG, "mhdgpu_batch_advance: null handle");
-    if (nsteps < 0) return bfail(MHD_ERR_ARG, "mhdgpu_batch_advance: nsteps < 0");
+    if (!bt) return bfail(MHD_ERR_ARG, resume ? "mhdgpu_batch_resume: null handle" : "mhdgpu_batch_advance: null handle");
+    if (nsteps < 0) return bfail(MHD_ERR_ARG, resume ? "mhdgpu_batch_resume: nsteps < 0" : "mhdgpu_batch_advance: nsteps < 0");
     for (int it = 0; it < nsteps; ++it) {
-        const int st = launch_step(*bt, (cudaStream_t)stream, nullptr, it == 0);
+        const int st = launch_step(*bt, (cudaStream_t)stream, nullptr, it == 0 && !(resume && bt->folded));
         if (st) return st;
+        bt->folded = true;
     }
     return MHD_OK;
+}
+
+int mhdgpu_batch_advance(mhdgpu_batch *bt, int nsteps, mhdgpu_stream_t stream)
+{
+    return batch_steps(bt, nsteps, false, stream);
+}
+
+int mhdgpu_batch_resume(mhdgpu_batch *bt, int nsteps, mhdgpu_stream_t stream)
+{
+    return batch_steps(bt, nsteps, true, stream);
 }
 
 int mhdgpu_batch_read_clocks(mhdgpu_batch *bt, mhdgpu_clock *clocks, mhdgpu_stream_t stream)

@@ -312,6 +312,8 @@ int mhdgpu_advance(float *u, float *b, int nx, int ny, int nz, int nsteps, doubl
 {
     if (nsteps < 0) return fail(MHD_ERR_ARG, "mhdgpu_advance: nsteps < 0");
     if (!d_clock) return fail(MHD_ERR_ARG, "mhdgpu_advance: null clock");
+    const bool resume = (cfl_mode & MHD_ADVANCE_RESUME) != 0;
+    cfl_mode &= ~MHD_ADVANCE_RESUME;
     if (!(cfl_number > 0.0)) return fail(MHD_ERR_ARG, "mhdgpu_advance: cfl_number must be > 0");
     if (cfl_mode != MHD_CFL_C && cfl_mode != MHD_CFL_AVERAGED)
         return fail(MHD_ERR_ARG, "mhdgpu_advance: bad cfl mode");
@@ -319,13 +321,14 @@ int mhdgpu_advance(float *u, float *b, int nx, int ny, int nz, int nsteps, doubl
         return fail(MHD_ERR_ARG, "mhdgpu_advance: bad path");
     cudaStream_t s = (cudaStream_t)stream;
     // The CFL reduction runs as its own pass before the first step of the
-    // call; every step's last fluid sweep folds the next step's reduction into
-    // the clock's word (a max, so the first pass of a later call, over the
-    // same state, changes nothing).
+    // call (unless the caller resumes); every step's last fluid sweep folds
+    // the next step's reduction into the clock's word (a max, so the first
+    // pass of a later call, over the same state, changes nothing).
     for (int it = 0; it < nsteps; ++it) {
+        const bool pass = it == 0 && !resume;
         {
-            ProfScope ps(MHD_KCLASS_CFL, it == 0 ? 2 : 1, s);
-            if (it == 0) MHD_CU(launch_cfl(u, b, nx, ny, nz, cfl_mode, &d_clock->cmax, s), "mhdgpu_advance");
+            ProfScope ps(MHD_KCLASS_CFL, pass ? 2 : 1, s);
+            if (pass) MHD_CU(launch_cfl(u, b, nx, ny, nz, cfl_mode, &d_clock->cmax, s), "mhdgpu_advance");
             MHD_CU(launch_clock(d_clock, cfl_number, tf, d_dt_log, s), "mhdgpu_advance");
         }
         int st = (path == MHD_PATH_FUSED)

@@ -21,6 +21,7 @@ MHD_ERR_UNPHYSICAL = 4
 MHD_ERR_NOMEM = 5
 MHD_CFL_C = 0
 MHD_CFL_AVERAGED = 1
+MHD_ADVANCE_RESUME = 0x100   # or'ed into cfl_mode of advance(): reuse the folded CFL word
 MHD_HEALTH_NONFINITE = 1
 MHD_HEALTH_DENSITY = 2
 MHD_HEALTH_PRESSURE = 4
@@ -42,7 +43,7 @@ EXPORTS = [
     "mhdgpu_diagnostics_scratch_bytes", "mhdgpu_diagnostics",
     "mhdgpu_read_state", "mhdgpu_write_state", "mhdgpu_write_result", "mhdgpu_write_check",
     "mhdgpu_batch_workspace_bytes", "mhdgpu_batch_create", "mhdgpu_batch_destroy",
-    "mhdgpu_batch_advance", "mhdgpu_batch_read_clocks", "mhdgpu_batch_set_schedule",
+    "mhdgpu_batch_advance", "mhdgpu_batch_resume", "mhdgpu_batch_read_clocks", "mhdgpu_batch_set_schedule",
     "mhdgpu_batch_get_schedule", "mhdgpu_batch_tune", "mhdgpu_batch_inject_stall",
     # include/mhdgpu_compat.h
     "fluidx", "advectbyzx", "transpose12", "transpose13", "calcfl", "copy_matrix",
@@ -113,6 +114,7 @@ def lib() -> C.CDLL:
             "mhdgpu_batch_create": (I, [P, I, P, P, P, D, I, P]),
             "mhdgpu_batch_destroy": (I, [P]),
             "mhdgpu_batch_advance": (I, [P, I, P]),
+            "mhdgpu_batch_resume": (I, [P, I, P]),
             "mhdgpu_batch_read_clocks": (I, [P, P, P]),
             "mhdgpu_batch_set_schedule": (I, [P, I, I, I]),
             "mhdgpu_batch_get_schedule": (I, [P, I, P, P]),
@@ -198,10 +200,13 @@ def step_fused(u, b, nx, ny, nz, d_dt, work, health=None, stream=None):
 
 
 def advance(u, b, nx, ny, nz, nsteps, cfl_number, cfl_mode, tf, clock, dt_log, work,
-            path=MHD_PATH_PLAIN, stream=None):
-    """clock: a torch uint8 CUDA tensor of sizeof(Clock) bytes (see new_clock)."""
+            path=MHD_PATH_PLAIN, stream=None, resume=False):
+    """clock: a torch uint8 CUDA tensor of sizeof(Clock) bytes (see new_clock).
+    resume: the first step takes the CFL speed folded into the clock by the
+    previous advance of this unchanged state (MHD_ADVANCE_RESUME)."""
+    mode = int(cfl_mode) | (MHD_ADVANCE_RESUME if resume else 0)
     _check(lib().mhdgpu_advance(_p(u), _p(b), nx, ny, nz, int(nsteps), float(cfl_number),
-                                int(cfl_mode), float(tf), _p(clock), _p(dt_log), _p(work),
+                                mode, float(tf), _p(clock), _p(dt_log), _p(work),
                                 int(path), _stream(stream)))
 
 
@@ -392,8 +397,11 @@ class Batch:
         _check(lib().mhdgpu_batch_create(C.byref(self.h), n, dims, us, bs, float(cfl_number),
                                          int(cfl_mode), tfa))
 
-    def advance(self, nsteps=1, stream=None):
-        _check(lib().mhdgpu_batch_advance(self.h, int(nsteps), _stream(stream)))
+    def advance(self, nsteps=1, stream=None, resume=False):
+        """resume: continue the previous advance of the unchanged boxes without
+        the first step's CFL pass (mhdgpu_batch_resume)."""
+        fn = lib().mhdgpu_batch_resume if resume else lib().mhdgpu_batch_advance
+        _check(fn(self.h, int(nsteps), _stream(stream)))
 
     def clocks(self, stream=None, check=True):
         """Synchronises and returns the boxes' Clock records; with check, raises on

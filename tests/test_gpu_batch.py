@@ -171,6 +171,48 @@ def test_batch_graph_replay(gpu):
     _same(got, ref)
 
 
+@pytest.mark.parametrize("path", [0, 1])
+def test_advance_resume_equals_one_call(gpu, path):
+    """One step per call with MHD_ADVANCE_RESUME after the first (the CFL speed
+    taken from the previous step's fold instead of a pass) ends where one
+    multi-step call ends, bit for bit, state and clock."""
+    import torch
+    d = (48, 32, 16)
+    u0, b0 = _states([d], seed=21)[0]
+    runs = []
+    for resume in (False, True):
+        du, db = dev(u0), dev(b0)
+        work = torch.empty(gpu.step_workspace_bytes(*d, path), dtype=torch.uint8, device="cuda")
+        clock = gpu.new_clock()
+        if resume:
+            gpu.advance(du, db, *d, 1, 0.7, 0, 0.0, clock, None, work, path)
+            for _ in range(3):
+                gpu.advance(du, db, *d, 1, 0.7, 0, 0.0, clock, None, work, path, resume=True)
+        else:
+            gpu.advance(du, db, *d, 4, 0.7, 0, 0.0, clock, None, work, path)
+        runs.append((host(du), host(db), gpu.read_clock(clock)))
+    _same([runs[1]], [runs[0]])
+    assert runs[1][2].iter == 4
+
+
+def test_batch_resume_equals_one_call(gpu):
+    """mhdgpu_batch_resume continues without the CFL pass and ends where one
+    multi-step mhdgpu_batch_advance ends; on a handle that has not advanced
+    yet it runs the pass (same result as advance)."""
+    dims = CLASS_BOXES
+    states = _states(dims, seed=17)
+    ref = _batched(gpu, states, dims, 3, 0.7)
+    boxes = [(dev(u), dev(b), d) for (u, b), d in zip(states, dims)]
+    bt = gpu.Batch(boxes, cfl_number=0.7)
+    bt.advance(1, resume=True)     # first call: no fold yet, the pass runs
+    bt.advance(1, resume=True)
+    bt.advance(1, resume=True)
+    clocks = bt.clocks()
+    got = [(host(u), host(b), c) for (u, b, _), c in zip(boxes, clocks)]
+    bt.close()
+    _same(got, ref)
+
+
 def test_batch_fast_math_matches_per_box(gpu):
     """The fast policy lets the compiler contract multiply-adds, and the
     contraction can differ between the single-box and the batched kernels in
