@@ -391,20 +391,26 @@ __device__ __forceinline__ void fluidx_tile_reg(const FluidxArgs &a, long long t
     // ---- write back: component-major shared rows -> the cell-major state ----
     if (!ROWS) {
         float *g = a.u_out + p0 * 5 * N;
-        const int nf = nvalid * 5 * N;   // a multiple of 4 (N is a multiple of 16)
         if ((reinterpret_cast<uintptr_t>(g) & 15u) == 0) {
-            for (int e4 = threadIdx.x; e4 < nf / 4; e4 += blockDim.x) {
-                int cell = (4 * e4) / 5, comp = 4 * e4 - 5 * cell;
-                float x[4];
+            // a group of 4 consecutive cells of one pencil: its five component
+            // runs are five 16-byte shared loads, its 20 floats five 16-byte
+            // stores (the transpose happens in registers)
+            const int ngroups = nvalid * (N / 4);
+            for (int gi = threadIdx.x; gi < ngroups; gi += blockDim.x) {
+                const int qq = gi / (N / 4), cc = 4 * (gi - qq * (N / 4));
+                const float *src = US + qq * PS + cc;
+                float4 c[5];
 #pragma unroll
-                for (int r = 0; r < 4; ++r) {
-                    const int qq = cell / N, cc = cell - qq * N;
-                    x[r] = US[qq * PS + comp * CS + cc];
-                    if (++comp == 5) { comp = 0; ++cell; }
-                }
-                reinterpret_cast<float4 *>(g)[e4] = make_float4(x[0], x[1], x[2], x[3]);
+                for (int ii = 0; ii < 5; ++ii) c[ii] = *reinterpret_cast<const float4 *>(src + ii * CS);
+                float4 *dst = reinterpret_cast<float4 *>(g + (size_t)(qq * N + cc) * 5);
+                dst[0] = make_float4(c[0].x, c[1].x, c[2].x, c[3].x);
+                dst[1] = make_float4(c[4].x, c[0].y, c[1].y, c[2].y);
+                dst[2] = make_float4(c[3].y, c[4].y, c[0].z, c[1].z);
+                dst[3] = make_float4(c[2].z, c[3].z, c[4].z, c[0].w);
+                dst[4] = make_float4(c[1].w, c[2].w, c[3].w, c[4].w);
             }
         } else {
+            const int nf = nvalid * 5 * N;
             for (int e = threadIdx.x; e < nf; e += blockDim.x) {
                 const int cell = e / 5, comp = e - 5 * cell, qq = cell / N, cc = cell - qq * N;
                 g[e] = US[qq * PS + comp * CS + cc];
