@@ -318,6 +318,14 @@ int mhdgpu_batch_advance(mhdgpu_batch *bt, int nsteps, mhdgpu_stream_t stream);
  * handle's last advance; the handle runs the pass anyway when it has not
  * advanced yet (or its schedule was tuned since). */
 int mhdgpu_batch_resume(mhdgpu_batch *bt, int nsteps, mhdgpu_stream_t stream);
+/* The host-buffer entry of the ensemble: uploads every box from h_u[i]
+ * (5 floats per cell) and h_b[i] (3 per cell), advances nsteps steps as
+ * mhdgpu_batch_advance does, downloads the boxes into the same buffers and
+ * synchronises stream.  The copies are spread over the handle's side streams
+ * so that several run at once; pinned host buffers copy fastest.  The boxes'
+ * device arrays given at creation are overwritten. */
+int mhdgpu_batch_run_host(mhdgpu_batch *bt, float *const *h_u, float *const *h_b, int nsteps,
+                          mhdgpu_stream_t stream);
 /* synchronises stream and copies the nbox clocks to the host; returns
  * MHD_ERR_TIMEOUT after a stall, MHD_ERR_UNPHYSICAL when a box's health
  * reports NaN/Inf or rho <= 0 */

@@ -492,6 +492,55 @@ int mhdgpu_batch_resume(mhdgpu_batch *bt, int nsteps, mhdgpu_stream_t stream)
     return batch_steps(bt, nsteps, true, stream);
 }
 
+// copies of every box between host and device, spread over the side streams
+// (several copy engines at once), forked from and joined back to s
+static int batch_copy_host(mhdgpu_batch &bt, float *const *h_u, float *const *h_b, bool to_device,
+                           cudaStream_t s)
+{
+    BCU(cudaEventRecord(bt.fork, s), "mhdgpu_batch_run_host fork");
+    const int ns = std::min(bt.nbox, kBatchClasses);
+    for (int k = 0; k < ns; ++k) BCU(cudaStreamWaitEvent(bt.side[k], bt.fork, 0), "mhdgpu_batch_run_host fork");
+    for (int i = 0; i < bt.nbox; ++i) {
+        const BoxDesc &d = bt.box[i];
+        const size_t nc = (size_t)d.nx * d.ny * d.nz;
+        cudaStream_t cs = bt.side[i % ns];
+        if (to_device) {
+            BCU(cudaMemcpyAsync(d.u, h_u[i], 5 * nc * sizeof(float), cudaMemcpyHostToDevice, cs), "mhdgpu_batch_run_host upload");
+            BCU(cudaMemcpyAsync(d.b, h_b[i], 3 * nc * sizeof(float), cudaMemcpyHostToDevice, cs), "mhdgpu_batch_run_host upload");
+        } else {
+            BCU(cudaMemcpyAsync(h_u[i], d.u, 5 * nc * sizeof(float), cudaMemcpyDeviceToHost, cs), "mhdgpu_batch_run_host download");
+            BCU(cudaMemcpyAsync(h_b[i], d.b, 3 * nc * sizeof(float), cudaMemcpyDeviceToHost, cs), "mhdgpu_batch_run_host download");
+        }
+    }
+    for (int k = 0; k < ns; ++k) {
+        BCU(cudaEventRecord(bt.join[k], bt.side[k]), "mhdgpu_batch_run_host join");
+        BCU(cudaStreamWaitEvent(s, bt.join[k], 0), "mhdgpu_batch_run_host join");
+    }
+    return MHD_OK;
+}
+
+int mhdgpu_batch_run_host(mhdgpu_batch *bt, float *const *h_u, float *const *h_b, int nsteps,
+                          mhdgpu_stream_t stream)
+{
+    if (!bt || !h_u || !h_b) return bfail(MHD_ERR_ARG, "mhdgpu_batch_run_host: null pointer");
+    if (nsteps < 0) return bfail(MHD_ERR_ARG, "mhdgpu_batch_run_host: nsteps < 0");
+    for (int i = 0; i < bt->nbox; ++i)
+        if (!h_u[i] || !h_b[i]) return bfail(MHD_ERR_ARG, "mhdgpu_batch_run_host: null box buffer");
+    cudaStream_t s = (cudaStream_t)stream;
+    int st = batch_copy_host(*bt, h_u, h_b, true, s);
+    if (st) return st;
+    // the state was just written from the host: the first step runs the CFL pass
+    for (int it = 0; it < nsteps; ++it) {
+        st = launch_step(*bt, s, nullptr, it == 0);
+        if (st) return st;
+        bt->folded = true;
+    }
+    st = batch_copy_host(*bt, h_u, h_b, false, s);
+    if (st) return st;
+    BCU(cudaStreamSynchronize(s), "mhdgpu_batch_run_host");
+    return MHD_OK;
+}
+
 int mhdgpu_batch_read_clocks(mhdgpu_batch *bt, mhdgpu_clock *clocks, mhdgpu_stream_t stream)
 {
     if (!bt || !clocks) return bfail(MHD_ERR_ARG, "mhdgpu_batch_read_clocks: null pointer");

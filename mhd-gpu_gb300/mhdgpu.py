@@ -43,7 +43,8 @@ EXPORTS = [
     "mhdgpu_diagnostics_scratch_bytes", "mhdgpu_diagnostics",
     "mhdgpu_read_state", "mhdgpu_write_state", "mhdgpu_write_result", "mhdgpu_write_check",
     "mhdgpu_batch_workspace_bytes", "mhdgpu_batch_create", "mhdgpu_batch_destroy",
-    "mhdgpu_batch_advance", "mhdgpu_batch_resume", "mhdgpu_batch_read_clocks", "mhdgpu_batch_set_schedule",
+    "mhdgpu_batch_advance", "mhdgpu_batch_resume", "mhdgpu_batch_run_host", "mhdgpu_batch_read_clocks",
+    "mhdgpu_batch_set_schedule",
     "mhdgpu_batch_get_schedule", "mhdgpu_batch_tune", "mhdgpu_batch_inject_stall",
     # include/mhdgpu_compat.h
     "fluidx", "advectbyzx", "transpose12", "transpose13", "calcfl", "copy_matrix",
@@ -115,6 +116,7 @@ def lib() -> C.CDLL:
             "mhdgpu_batch_destroy": (I, [P]),
             "mhdgpu_batch_advance": (I, [P, I, P]),
             "mhdgpu_batch_resume": (I, [P, I, P]),
+            "mhdgpu_batch_run_host": (I, [P, P, P, I, P]),
             "mhdgpu_batch_read_clocks": (I, [P, P, P]),
             "mhdgpu_batch_set_schedule": (I, [P, I, I, I]),
             "mhdgpu_batch_get_schedule": (I, [P, I, P, P]),
@@ -139,6 +141,16 @@ def _check(status: int):
 
 def _p(t):
     return None if t is None else C.c_void_p(t.data_ptr())
+
+
+def _host_ptr(x):
+    """Address of a host float32 buffer: a CPU tensor (pinned or not) or a
+    C-contiguous numpy array."""
+    if hasattr(x, "data_ptr"):
+        assert not x.is_cuda and x.is_contiguous()
+        return x.data_ptr()
+    assert x.flags["C_CONTIGUOUS"]
+    return x.ctypes.data
 
 
 def _stream(stream=None):
@@ -402,6 +414,15 @@ class Batch:
         the first step's CFL pass (mhdgpu_batch_resume)."""
         fn = lib().mhdgpu_batch_resume if resume else lib().mhdgpu_batch_advance
         _check(fn(self.h, int(nsteps), _stream(stream)))
+
+    def run_host(self, host_u, host_b, nsteps=1, stream=None):
+        """Uploads every box from host_u[i], host_b[i] (CPU float32 arrays or
+        tensors, pinned for speed), advances nsteps steps, downloads into the
+        same buffers and synchronises (mhdgpu_batch_run_host)."""
+        n = len(self.boxes)
+        hu = (C.c_void_p * n)(*[_host_ptr(x) for x in host_u])
+        hb = (C.c_void_p * n)(*[_host_ptr(x) for x in host_b])
+        _check(lib().mhdgpu_batch_run_host(self.h, hu, hb, int(nsteps), _stream(stream)))
 
     def clocks(self, stream=None, check=True):
         """Synchronises and returns the boxes' Clock records; with check, raises on

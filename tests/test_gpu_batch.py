@@ -213,6 +213,29 @@ def test_batch_resume_equals_one_call(gpu):
     _same(got, ref)
 
 
+def test_batch_run_host_equals_device_path(gpu):
+    """mhdgpu_batch_run_host (upload, steps, download, from pinned and from
+    pageable host buffers) ends where the device path ends, bit for bit."""
+    import torch
+    dims = CLASS_BOXES
+    states = _states(dims, seed=23)
+    ref = _batched(gpu, states, dims, 2, 0.7)
+    for pinned in (True, False):
+        boxes = [(dev(np.zeros_like(u)), dev(np.zeros_like(b)), d) for (u, b), d in zip(states, dims)]
+        bt = gpu.Batch(boxes, cfl_number=0.7)
+        hu = [torch.from_numpy(u.copy()) for u, _ in states]
+        hb = [torch.from_numpy(b.copy()) for _, b in states]
+        if pinned:
+            hu = [x.pin_memory() for x in hu]
+            hb = [x.pin_memory() for x in hb]
+        bt.run_host(hu, hb, 1)
+        bt.run_host(hu, hb, 1)
+        clocks = bt.clocks()
+        got = [(x.numpy(), y.numpy(), c) for x, y, c in zip(hu, hb, clocks)]
+        bt.close()
+        _same(got, ref)
+
+
 def test_batch_fast_math_matches_per_box(gpu):
     """The fast policy lets the compiler contract multiply-adds, and the
     contraction can differ between the single-box and the batched kernels in
