@@ -569,7 +569,7 @@ def main():
             bt = mhdgpu.Batch(boxes, cfl_number=CFL, cfl_mode=mhdgpu.MHD_CFL_C)
             if tune:
                 bt.tune(stream=stream)
-            g = capture(lambda: bt.advance(1, stream=stream), stream, 2)
+            g = capture(lambda: bt.advance(1, stream=stream, resume=True), stream, 2)
             cells = total
         else:
             u0, b0 = ics.alfven_oblique(n)
@@ -578,8 +578,13 @@ def main():
             clock = mhdgpu.new_clock(device=dev)
             if tune:
                 mhdgpu.autotune(n, n, n, math_mode)
-            g = capture(lambda: mhdgpu.advance(du, db, n, n, n, 1, CFL, 0, 0.0, clock, None, work, 1),
-                        stream, 2)
+            started = [False]
+
+            def one_step():
+                mhdgpu.advance(du, db, n, n, n, 1, CFL, 0, 0.0, clock, None, work, 1, resume=started[0])
+                started[0] = True
+
+            g = capture(one_step, stream, 2)
             cells = world * n ** 3
         secs, wall = timed_replays(g.replay, K, W, stream, flush, world)
         sampler.stop()
