@@ -375,11 +375,11 @@ __device__ __forceinline__ void fluidx_tile_team(const FluidxArgs &a, long long 
 // One CTA's work on a tile; called once per CTA by fluidx_kernel and in a loop
 // by the batched kernel (batch_kernel.cuh).  Pencils that fill a team of at
 // most one warp exactly take the register-blocked tile (same results).
-template <int CPL, int WPP, class M, bool ROWS, int NT>
+template <int CPL, int WPP, class M, bool ROWS, int NT, bool GROUPED = false>
 __device__ __forceinline__ void fluidx_tile(const FluidxArgs &a, long long tile)
 {
     if constexpr (NT > 0 && reg_tile_shape(NT, CPL, WPP))
-        fluidx_tile_reg<CPL, team_threads<WPP>(), M, ROWS>(a, tile);
+        fluidx_tile_reg<CPL, team_threads<WPP>(), M, ROWS, GROUPED>(a, tile);
     else
         fluidx_tile_team<CPL, WPP, M, ROWS, NT>(a, tile);
 }
@@ -388,7 +388,7 @@ template <int CPL, int WPP, class M, bool ROWS, int NT>
 __global__ void __launch_bounds__(256)
 fluidx_kernel(FluidxArgs a)
 {
-    fluidx_tile<CPL, WPP, M, ROWS, NT>(a, blockIdx.x);
+    fluidx_tile<CPL, WPP, M, ROWS, NT, true>(a, blockIdx.x);
 }
 
 // Launch one instantiation; sets the dynamic shared-memory attribute once per

@@ -107,7 +107,10 @@ __device__ __forceinline__ void load_comp(const float *p, bool live, int ii, flo
     }
 }
 
-template <int CPL, int TPP, class M, bool ROWS>
+// GROUPED: rows mode moves its rows in groups of four with per-lane offsets
+// fixed for the tile (fewer copy instructions, more registers held); the
+// single-box kernels take it, the register-capped batch kernels do not.
+template <int CPL, int TPP, class M, bool ROWS, bool GROUPED = false>
 __device__ __forceinline__ void fluidx_tile_reg(const FluidxArgs &a, long long tile)
 {
     constexpr int N = TPP * CPL;
@@ -178,37 +181,89 @@ __device__ __forceinline__ void fluidx_tile_reg(const FluidxArgs &a, long long t
             const long long kpb = (long long)kp * f.sk;
             float *SB = BS;                          // (ppc+1) * BSR: b of columns j0 .. j0+nvalid
             float *SK = BS + (ppc + 1) * BSR;        // ppc * KS: b(3) of plane k+1, [pencil][i]
-            const int ru = 5 * nvalid, rb = 3 * (nvalid + 1);
-            const int pb2 = nib(f.pb, 2);
-            // per-lane offsets, independent of the row: a row of u is ru floats
-            // at u_in + (rowc + j0)*5, element r -> pencil r/5, stored component r%5
-            int us_off[2], sb_off[2], gb_off[2];
-            bool us_on[2], sb_on[2];
-#pragma unroll
-            for (int h = 0; h < 2; ++h) {
-                const int r = lane + 32 * h;
-                us_on[h] = r < ru;
-                const int qq = r / 5, p = r - qq * 5;
-                us_off[h] = qq * PS + nib(f.iu, p) * CS;
-                sb_on[h] = r < rb;
-                const int qb = r / 3, pp = r - qb * 3;
-                int j = j0 + qb;
-                if (j >= f.ny) j -= f.ny;
-                sb_off[h] = qb * BSR + nib(f.ib, pp);
-                gb_off[h] = j * 3 + pp;
-            }
-            const bool sk_on = lane < nvalid;
-            for (int i = warp; i < N; i += nwarps) {
-                const long long rowc = kb + (long long)i * f.si;    // cell of (i, 0, k)
-                const float *gu = a.u_in + (rowc + j0) * 5;
-                const float *gb = a.b + rowc * 3;
-#pragma unroll
-                for (int h = 0; h < 2; ++h) {
-                    if (us_on[h]) cp_async4(&US[us_off[h] + i], gu + lane + 32 * h);
-                    if (sb_on[h]) cp_async4(&SB[sb_off[h] + i * 3], gb + gb_off[h]);
+            if constexpr (GROUPED) {
+                const int ru = 5 * nvalid, rb = 3 * (nvalid + 1);
+                const int pb2 = nib(f.pb, 2);
+                // Groups of 4 rows (cells i0 .. i0+3 of the tile's pencils, N is a
+                // multiple of 4).  A row holds ru floats of u at u_in + (row cell +
+                // j0)*5, rb floats of b (columns j0 .. j0+nvalid, the last one
+                // periodic) and nvalid b(3) values of plane k+1.  Each source takes
+                // its own passes of the warp (u: 4 ru <= 160 floats in five, b:
+                // 4 rb <= 108 in four, plane k+1: 4 nvalid <= 32 in one); lane e of
+                // pass s moves element 32 s + e of its source, at offsets from the
+                // group's first row that are fixed per lane.
+                int uso[5], ugo[5], bso[4], bgo[4];
+                bool uon[5], bon[4];
+    #pragma unroll
+                for (int s = 0; s < 5; ++s) {
+                    const int e = lane + 32 * s;
+                    const int ro = e / ru, r = e - ro * ru;
+                    const int qq = r / 5, p = r - qq * 5;
+                    uon[s] = ro < 4;
+                    uso[s] = uon[s] ? qq * PS + nib(f.iu, p) * CS + ro : 0;
+                    ugo[s] = uon[s] ? (int)(ro * f.si + j0) * 5 + r : 0;
                 }
-                if (sk_on)
-                    cp_async4(&SK[lane * KS + i], a.b + (kpb + (long long)i * f.si + j0 + lane) * 3 + pb2);
+    #pragma unroll
+                for (int s = 0; s < 4; ++s) {
+                    const int e = lane + 32 * s;
+                    const int ro = e / rb, r = e - ro * rb;
+                    const int qb = r / 3, pp = r - qb * 3;
+                    int j = j0 + qb;
+                    if (j >= f.ny) j -= f.ny;
+                    bon[s] = ro < 4;
+                    bso[s] = bon[s] ? qb * BSR + nib(f.ib, pp) + 3 * ro : 0;
+                    bgo[s] = bon[s] ? (int)(ro * f.si + j) * 3 + pp : 0;
+                }
+                const int kro = lane / nvalid, kqq = lane - kro * nvalid;
+                const bool kon = kro < 4;
+                const int kso = kon ? kqq * KS + kro : 0;
+                const int kgo = kon ? (int)(kro * f.si + j0 + kqq) * 3 + pb2 : 0;
+                for (int i0 = 4 * warp; i0 < N; i0 += 4 * nwarps) {
+                    const long long rowc = kb + (long long)i0 * f.si;    // cell of (i0, 0, k)
+                    const float *gu = a.u_in + rowc * 5;
+                    const float *gb = a.b + rowc * 3;
+                    const float *gk = a.b + (kpb + (long long)i0 * f.si) * 3;
+    #pragma unroll
+                    for (int s = 0; s < 5; ++s)
+                        if (uon[s]) cp_async4(&US[uso[s] + i0], gu + ugo[s]);
+    #pragma unroll
+                    for (int s = 0; s < 4; ++s)
+                        if (bon[s]) cp_async4(&SB[bso[s] + 3 * i0], gb + bgo[s]);
+                    if (kon) cp_async4(&SK[kso + i0], gk + kgo);
+                }
+            } else {
+                const int ru = 5 * nvalid, rb = 3 * (nvalid + 1);
+                const int pb2 = nib(f.pb, 2);
+                // per-lane offsets, independent of the row: a row of u is ru floats
+                // at u_in + (rowc + j0)*5, element r -> pencil r/5, stored component r%5
+                int us_off[2], sb_off[2], gb_off[2];
+                bool us_on[2], sb_on[2];
+    #pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const int r = lane + 32 * h;
+                    us_on[h] = r < ru;
+                    const int qq = r / 5, p = r - qq * 5;
+                    us_off[h] = qq * PS + nib(f.iu, p) * CS;
+                    sb_on[h] = r < rb;
+                    const int qb = r / 3, pp = r - qb * 3;
+                    int j = j0 + qb;
+                    if (j >= f.ny) j -= f.ny;
+                    sb_off[h] = qb * BSR + nib(f.ib, pp);
+                    gb_off[h] = j * 3 + pp;
+                }
+                const bool sk_on = lane < nvalid;
+                for (int i = warp; i < N; i += nwarps) {
+                    const long long rowc = kb + (long long)i * f.si;    // cell of (i, 0, k)
+                    const float *gu = a.u_in + (rowc + j0) * 5;
+                    const float *gb = a.b + rowc * 3;
+    #pragma unroll
+                    for (int h = 0; h < 2; ++h) {
+                        if (us_on[h]) cp_async4(&US[us_off[h] + i], gu + lane + 32 * h);
+                        if (sb_on[h]) cp_async4(&SB[sb_off[h] + i * 3], gb + gb_off[h]);
+                    }
+                    if (sk_on)
+                        cp_async4(&SK[lane * KS + i], a.b + (kpb + (long long)i * f.si + j0 + lane) * 3 + pb2);
+                }
             }
             cp_async_wait_all();
             __syncthreads();
@@ -417,22 +472,47 @@ __device__ __forceinline__ void fluidx_tile_reg(const FluidxArgs &a, long long t
             }
         }
     } else {
-        const long long kb = (long long)k * f.sk;
-        const int ru = 5 * nvalid;
-        int off[2];
-        bool on[2];
-#pragma unroll
-        for (int h = 0; h < 2; ++h) {
-            const int r = lane + 32 * h;
-            on[h] = r < ru;
-            const int qq = r / 5, p = r - qq * 5;
-            off[h] = qq * PS + nib(f.iu, p) * CS;
-        }
-        for (int i = warp; i < N; i += nwarps) {
-            float *g = a.u_out + (kb + (long long)i * f.si + j0) * 5;
-#pragma unroll
-            for (int h = 0; h < 2; ++h)
-                if (on[h]) g[lane + 32 * h] = US[off[h] + i];
+        if constexpr (GROUPED) {
+            // groups of 4 rows: a row is ru = 5*nvalid consecutive floats at
+            // u_out + (row cell + j0)*5; the 4*ru <= 160 floats of a group take
+            // five passes of a warp, each lane with fixed (row, pencil, component)
+            const long long kb = (long long)k * f.sk;
+            const int ru = 5 * nvalid;
+            int so[5], go[5];
+            bool on[5];
+    #pragma unroll
+            for (int s = 0; s < 5; ++s) {
+                const int e = lane + 32 * s;
+                const int ro = e / ru, r = e - ro * ru;
+                const int qq = r / 5, p = r - qq * 5;
+                on[s] = ro < 4;
+                so[s] = on[s] ? qq * PS + nib(f.iu, p) * CS + ro : 0;
+                go[s] = on[s] ? (int)(ro * f.si + j0) * 5 + r : 0;
+            }
+            for (int i0 = 4 * warp; i0 < N; i0 += 4 * nwarps) {
+                float *g = a.u_out + (kb + (long long)i0 * f.si) * 5;
+    #pragma unroll
+                for (int s = 0; s < 5; ++s)
+                    if (on[s]) g[go[s]] = US[so[s] + i0];
+            }
+        } else {
+            const long long kb = (long long)k * f.sk;
+            const int ru = 5 * nvalid;
+            int off[2];
+            bool on[2];
+    #pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int r = lane + 32 * h;
+                on[h] = r < ru;
+                const int qq = r / 5, p = r - qq * 5;
+                off[h] = qq * PS + nib(f.iu, p) * CS;
+            }
+            for (int i = warp; i < N; i += nwarps) {
+                float *g = a.u_out + (kb + (long long)i * f.si + j0) * 5;
+    #pragma unroll
+                for (int h = 0; h < 2; ++h)
+                    if (on[h]) g[lane + 32 * h] = US[off[h] + i];
+            }
         }
     }
 }
