@@ -17,7 +17,9 @@
 // Stage B reads only the pre-advection b(3) and u, so fusing A and B in one
 // kernel changes no value.  Pencils that run across memory (the y and z
 // sweeps of an x-major box) are staged through shared memory in rows, as in
-// fluidx_kernel.cuh.
+// fluidx_kernel.cuh.  Pencils of 32, 48, 64, 96 or 128 cells take the
+// register-blocked tile of advect_reg.cuh, every other length the team tile
+// below (same arithmetic).
 #pragma once
 
 #include "advect_reg.cuh"

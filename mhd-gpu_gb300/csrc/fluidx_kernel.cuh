@@ -18,12 +18,16 @@
 //     PPC neighbouring pencils at one k, so each cell i of them is one
 //     contiguous row of PPC cells, and rows are moved with consecutive lanes
 //     on consecutive addresses (the transpose happens in shared memory).
-// Each pencil belongs to a team of 32*WPP threads, CPL cells per thread
-// (cell c = m*32*WPP + t).  Stencil neighbours (i-1, i+1, i+2) go through a
-// per-pencil shared buffer; the two pencil-wide maxima of the fast speed are
-// warp-shuffle reductions (plus one shared step when WPP > 1).  No tensor
-// cores: nothing on this path is a contraction; the kernel is bounded by FP32
-// issue.
+// Two tiles with the same arithmetic: for pencils that fill a team of at most
+// one warp exactly (32, 48, 64, 96, 128 cells) the register-blocked tile of
+// fluidx_reg.cuh (thread t owns consecutive cells, neighbours by warp
+// shuffle); for every other length the team tile below, where each pencil
+// belongs to a team of 32*WPP threads, CPL cells per thread (cell
+// c = m*32*WPP + t), stencil neighbours (i-1, i+1, i+2) go through a
+// per-pencil shared buffer and the two pencil-wide maxima of the fast speed
+// are warp-shuffle reductions (plus one shared step when WPP > 1).  No tensor
+// cores: nothing on this path is a contraction; the kernel is bounded by
+// instruction issue.
 #pragma once
 
 #include "fluidx_reg.cuh"
