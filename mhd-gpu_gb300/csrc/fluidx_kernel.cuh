@@ -347,7 +347,7 @@ __device__ __forceinline__ void fluidx_tile_team(const FluidxArgs &a, long long 
                 }
             }
         }
-        if (fold_cfl) cfl_block_max(cfl_c, a.cfl);   // every thread of the CTA (a.cfl is uniform)
+        if (fold_cfl) cfl_warp_max(cfl_c, a.cfl);   // every lane of the warp
     }
 
     if (!live) bad = 0;

@@ -194,7 +194,7 @@ __device__ __forceinline__ void fluidx_tile_reg(const FluidxArgs &a, long long t
                 // group's first row that are fixed per lane.
                 int uso[5], ugo[5], bso[4], bgo[4];
                 bool uon[5], bon[4];
-    #pragma unroll
+#pragma unroll
                 for (int s = 0; s < 5; ++s) {
                     const int e = lane + 32 * s;
                     const int ro = e / ru, r = e - ro * ru;
@@ -203,7 +203,7 @@ __device__ __forceinline__ void fluidx_tile_reg(const FluidxArgs &a, long long t
                     uso[s] = uon[s] ? qq * PS + nib(f.iu, p) * CS + ro : 0;
                     ugo[s] = uon[s] ? (int)(ro * f.si + j0) * 5 + r : 0;
                 }
-    #pragma unroll
+#pragma unroll
                 for (int s = 0; s < 4; ++s) {
                     const int e = lane + 32 * s;
                     const int ro = e / rb, r = e - ro * rb;
@@ -223,10 +223,10 @@ __device__ __forceinline__ void fluidx_tile_reg(const FluidxArgs &a, long long t
                     const float *gu = a.u_in + rowc * 5;
                     const float *gb = a.b + rowc * 3;
                     const float *gk = a.b + (kpb + (long long)i0 * f.si) * 3;
-    #pragma unroll
+#pragma unroll
                     for (int s = 0; s < 5; ++s)
                         if (uon[s]) cp_async4(&US[uso[s] + i0], gu + ugo[s]);
-    #pragma unroll
+#pragma unroll
                     for (int s = 0; s < 4; ++s)
                         if (bon[s]) cp_async4(&SB[bso[s] + 3 * i0], gb + bgo[s]);
                     if (kon) cp_async4(&SK[kso + i0], gk + kgo);
@@ -238,7 +238,7 @@ __device__ __forceinline__ void fluidx_tile_reg(const FluidxArgs &a, long long t
                 // at u_in + (rowc + j0)*5, element r -> pencil r/5, stored component r%5
                 int us_off[2], sb_off[2], gb_off[2];
                 bool us_on[2], sb_on[2];
-    #pragma unroll
+#pragma unroll
                 for (int h = 0; h < 2; ++h) {
                     const int r = lane + 32 * h;
                     us_on[h] = r < ru;
@@ -256,7 +256,7 @@ __device__ __forceinline__ void fluidx_tile_reg(const FluidxArgs &a, long long t
                     const long long rowc = kb + (long long)i * f.si;    // cell of (i, 0, k)
                     const float *gu = a.u_in + (rowc + j0) * 5;
                     const float *gb = a.b + rowc * 3;
-    #pragma unroll
+#pragma unroll
                     for (int h = 0; h < 2; ++h) {
                         if (us_on[h]) cp_async4(&US[us_off[h] + i], gu + lane + 32 * h);
                         if (sb_on[h]) cp_async4(&SB[sb_off[h] + i * 3], gb + gb_off[h]);
@@ -436,7 +436,7 @@ __device__ __forceinline__ void fluidx_tile_reg(const FluidxArgs &a, long long t
                     }
                 }
             }
-            cfl_block_max(cfl_c, a.cfl);   // every thread of the CTA (a.cfl is uniform)
+            cfl_warp_max(cfl_c, a.cfl);   // every lane of the warp
         }
     }
 
@@ -480,7 +480,7 @@ __device__ __forceinline__ void fluidx_tile_reg(const FluidxArgs &a, long long t
             const int ru = 5 * nvalid;
             int so[5], go[5];
             bool on[5];
-    #pragma unroll
+#pragma unroll
             for (int s = 0; s < 5; ++s) {
                 const int e = lane + 32 * s;
                 const int ro = e / ru, r = e - ro * ru;
@@ -491,7 +491,7 @@ __device__ __forceinline__ void fluidx_tile_reg(const FluidxArgs &a, long long t
             }
             for (int i0 = 4 * warp; i0 < N; i0 += 4 * nwarps) {
                 float *g = a.u_out + (kb + (long long)i0 * f.si) * 5;
-    #pragma unroll
+#pragma unroll
                 for (int s = 0; s < 5; ++s)
                     if (on[s]) g[go[s]] = US[so[s] + i0];
             }
@@ -500,7 +500,7 @@ __device__ __forceinline__ void fluidx_tile_reg(const FluidxArgs &a, long long t
             const int ru = 5 * nvalid;
             int off[2];
             bool on[2];
-    #pragma unroll
+#pragma unroll
             for (int h = 0; h < 2; ++h) {
                 const int r = lane + 32 * h;
                 on[h] = r < ru;
@@ -509,7 +509,7 @@ __device__ __forceinline__ void fluidx_tile_reg(const FluidxArgs &a, long long t
             }
             for (int i = warp; i < N; i += nwarps) {
                 float *g = a.u_out + (kb + (long long)i * f.si + j0) * 5;
-    #pragma unroll
+#pragma unroll
                 for (int h = 0; h < 2; ++h)
                     if (on[h]) g[lane + 32 * h] = US[off[h] + i];
             }

@@ -201,6 +201,17 @@ __device__ __forceinline__ void cfl_block_max(float cl, unsigned *cmax)
     __syncthreads();
 }
 
+// The same fold from one warp, without a CTA barrier: a warp max, then one
+// atomicMax by lane 0 unless the word already holds as much (a stale read only
+// costs an extra atomic).  Every lane of the warp calls it.
+__device__ __forceinline__ void cfl_warp_max(float cl, unsigned *cmax)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) cl = fmaxf(cl, __shfl_xor_sync(0xffffffffu, cl, o));
+    if ((threadIdx.x & 31) == 0 && cl > __uint_as_float(*(volatile unsigned *)cmax))
+        atomicMax(cmax, __float_as_uint(cl));
+}
+
 // Device health word bits (also in include/mhdgpu.h).
 __device__ __forceinline__ void flag_health(unsigned *health, unsigned bits)
 {

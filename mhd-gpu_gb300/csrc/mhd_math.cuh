@@ -264,19 +264,26 @@ MHD_HD void cell_flux(const float u[5], const float bc[3], float v[5], float &cs
 MHD_HD float cfl_speed_c(const float u[5], const float b[3])
 {
     const float r = u[0], m1 = u[1], m2 = u[2], m3 = u[3], e = u[4];
-    const float t1 = fabsf(fdiv(m1, r)), t2 = fabsf(fdiv(m2, r)), t3 = fabsf(fdiv(m3, r));
+    // The five quotients by rho share one correctly rounded reciprocal with
+    // Markstein's correction (Faithful::divy: the IEEE quotient for normal
+    // operands, as in the fluxes); a density that is not a positive finite
+    // number takes the IEEE divisions, so inf and NaN propagate as before.
+    const bool mk = r > 0.0f && r <= 3.40282347e38f;
+    const float yr = mk ? Faithful::recip(r) : 0.0f;
+    auto qdiv = [&](float x) { return mk ? Faithful::divy(x, r, yr) : fdiv(x, r); };
+    const float t1 = fabsf(qdiv(m1)), t2 = fabsf(qdiv(m2)), t3 = fabsf(qdiv(m3));
     float v;
     if (t1 > t2) v = (t1 > t3) ? t1 : t3; else v = (t2 > t3) ? t2 : t3;
     const float b2 = fadd(fadd(fmul(b[0], b[0]), fmul(b[1], b[1])), fmul(b[2], b[2]));
     const float s2 = fadd(fadd(fmul(m1, m1), fmul(m2, m2)), fmul(m3, m3));
-    const float ps = total_pressure(e, fdiv(s2, r), b2);
+    const float ps = total_pressure(e, qdiv(s2), b2);
     const float p = fsub(ps, 0.5f * b2);
     const float gp = fmul(kGamma, p);
     // X = 2*B2 + gp exactly as a float pair, then |X| / r in float-float
     float xh, xl;
     two_sum(2.0f * b2, gp, xh, xl);
     if (xh < 0.0f) { xh = -xh; xl = -xl; }
-    const float yh = fdiv(xh, r);
+    const float yh = qdiv(xh);
     const float rem = ffma(-yh, r, xh);                 // exact remainder
     const float yl = fdiv_approx(fadd(rem, xl), r);
     // sqrt(yh + yl) + v
