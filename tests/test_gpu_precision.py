@@ -151,6 +151,17 @@ def test_lowbeta_blast_study_128(gpu, oracle_lib):
         assert r["health"] & (gpu.MHD_HEALTH_NONFINITE | gpu.MHD_HEALTH_DENSITY) == 0
 
 
+@pytest.mark.slow
+@pytest.mark.skipif(not SLOW, reason="full-size study: set MHDGPU_SLOW=1")
+def test_lowbeta_blast_study_256(gpu, oracle_lib):
+    """Config 5 at its full size (256^3, 300 steps); the FP64 oracle replays
+    each run's dt sequence on the host cores (about 5e9 FP64 cell-updates)."""
+    res = _blast_study(gpu, oracle_lib, 256, 300, threads=os.cpu_count())
+    print("LOWBETA_STUDY_256", res)
+    for r in res.values():
+        assert r["health"] & (gpu.MHD_HEALTH_NONFINITE | gpu.MHD_HEALTH_DENSITY) == 0
+
+
 def _turbulence_study(gpu, oracle_lib, n, nsteps, threads=None):
     import ics
     dims = (n, n, n)
