@@ -162,6 +162,16 @@ int mhdgpu_step_fused(float *u, float *b, int nx, int ny, int nz, const float *d
 
 #define MHD_PATH_PLAIN      0   /* mhdgpu_step: per-subroutine kernels + transposes */
 #define MHD_PATH_FUSED      1   /* mhdgpu_step_fused: transpose-free */
+#define MHD_PATH_AUTO       2   /* the faster of the two for the box (mhdgpu_resolve_path) */
+
+/* The path MHD_PATH_AUTO takes for an nx*ny*nz box: MHD_PATH_FUSED when
+ * every y and z pencil has at most 128 cells or exactly 256 (their sweeps
+ * stage whole rows of pencils efficiently), else MHD_PATH_PLAIN (measured on
+ * GB300: at 512^3 the plain step is 1.6x faster, at 128^3 the transpose-free
+ * one 1.15x).  mhdgpu_path_workspace_bytes sizes the workspace of a path
+ * (MHD_PATH_AUTO: of the path it takes). */
+int mhdgpu_resolve_path(int nx, int ny, int nz);
+size_t mhdgpu_path_workspace_bytes(int nx, int ny, int nz, int path);
 
 /* clock of a run kept on the device */
 typedef struct {
@@ -179,7 +189,8 @@ typedef struct {
  * step's dt at d_dt_log[clock.iter], so it must hold clock.iter + nsteps
  * entries.  Steps with tf > 0 and t >= tf are skipped on the device (the
  * reference's do-while exit).  path = MHD_PATH_PLAIN (d_work of
- * mhdgpu_step_workspace_bytes) or MHD_PATH_FUSED (of
+ * mhdgpu_step_workspace_bytes), MHD_PATH_AUTO (of mhdgpu_path_workspace_bytes)
+ * or MHD_PATH_FUSED (of
  * mhdgpu_step_fused_workspace_bytes).
  *
  * The CFL reduction runs as its own pass over the state before the call's

@@ -25,6 +25,7 @@ PencilCfg advect_pick(int n)
     if (n <= 32)  return {1, 1, 8};
     if (n <= 64)  return {2, 1, 4};
     if (n <= 128) return {4, 1, 4};
+    if (n == 256) return {2, 4, 1};
     if (n <= 256) return {4, 2, 2};
     if (n <= 512) return {4, 4, 1};
     return {4, 8, 1};

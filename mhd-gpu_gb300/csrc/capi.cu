@@ -306,6 +306,20 @@ static int step_fused(float *u, float *b, int nx, int ny, int nz, const float *d
     return sweep_view(u, b, fx, d_dt, scr, d_health, false, s, cfl, cfl_mode);
 }
 
+int mhdgpu_resolve_path(int nx, int ny, int nz)
+{
+    auto staged = [](int n) { return n <= 128 || n == 256; };
+    return (staged(ny) && staged(nz)) ? MHD_PATH_FUSED : MHD_PATH_PLAIN;
+}
+
+size_t mhdgpu_path_workspace_bytes(int nx, int ny, int nz, int path)
+{
+    if (path == MHD_PATH_AUTO) path = mhdgpu_resolve_path(nx, ny, nz);
+    if (path == MHD_PATH_FUSED) return mhdgpu_step_fused_workspace_bytes(nx, ny, nz);
+    if (path == MHD_PATH_PLAIN) return mhdgpu_step_workspace_bytes(nx, ny, nz);
+    return 0;
+}
+
 int mhdgpu_advance(float *u, float *b, int nx, int ny, int nz, int nsteps, double cfl_number,
                    int cfl_mode, float tf, mhdgpu_clock *d_clock, float *d_dt_log, void *d_work,
                    int path, mhdgpu_stream_t stream)
@@ -317,6 +331,7 @@ int mhdgpu_advance(float *u, float *b, int nx, int ny, int nz, int nsteps, doubl
     if (!(cfl_number > 0.0)) return fail(MHD_ERR_ARG, "mhdgpu_advance: cfl_number must be > 0");
     if (cfl_mode != MHD_CFL_C && cfl_mode != MHD_CFL_AVERAGED)
         return fail(MHD_ERR_ARG, "mhdgpu_advance: bad cfl mode");
+    if (path == MHD_PATH_AUTO) path = mhdgpu_resolve_path(nx, ny, nz);
     if (path != MHD_PATH_PLAIN && path != MHD_PATH_FUSED)
         return fail(MHD_ERR_ARG, "mhdgpu_advance: bad path");
     cudaStream_t s = (cudaStream_t)stream;
@@ -348,6 +363,7 @@ int mhdgpu_run_host(float *u, float *b, int nx, int ny, int nz, double cfl_numbe
     if (st) return st;
     if (!u || !b || !t) return fail(MHD_ERR_ARG, "mhdgpu_run_host: null pointer");
     if (max_steps < 0) return fail(MHD_ERR_ARG, "mhdgpu_run_host: max_steps < 0");
+    if (path == MHD_PATH_AUTO) path = mhdgpu_resolve_path(nx, ny, nz);
     if (path != MHD_PATH_PLAIN && path != MHD_PATH_FUSED)
         return fail(MHD_ERR_ARG, "mhdgpu_run_host: bad path");
     const size_t ncell = (size_t)nx * ny * nz;

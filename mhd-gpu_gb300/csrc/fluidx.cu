@@ -11,6 +11,7 @@ PencilCfg fluidx_pick(int n)
     if (n <= 32)  return {1, 1, 8};
     if (n <= 64)  return {2, 1, 4};
     if (n <= 128) return {4, 1, 4};
+    if (n == 256) return {8, 1, 1};   // register-blocked, 8 cells per thread
     if (n <= 256) return {4, 2, 2};
     if (n <= 512) return {4, 4, 1};
     return {4, 8, 1};

@@ -55,7 +55,7 @@ struct PencilCfg { int cpl, wpp, ppc; };
 
 // the (CPL, WPP) pairs that are compiled
 #define MHD_PENCIL_SHAPES(X) \
-    X(1, 1) X(2, 1) X(4, 1) X(1, 2) X(2, 2) X(4, 2) X(1, 4) X(2, 4) X(4, 4) X(2, 8) X(4, 8)
+    X(1, 1) X(2, 1) X(4, 1) X(8, 1) X(1, 2) X(2, 2) X(4, 2) X(1, 4) X(2, 4) X(4, 4) X(2, 8) X(4, 8)
 
 inline bool pencil_shape_ok(const PencilCfg &c, int n)
 {
@@ -73,7 +73,7 @@ bool frame_supported(const Frame &f);
 // pencils across memory): the tuned one if the autotuner (or mhdgpu_set_tile)
 // recorded it, else the default table
 PencilCfg pencil_cfg(int kclass, int n, bool rows = false);
-PencilCfg rows_pick(int n);
+PencilCfg rows_pick(int kclass, int n);
 int math_mode();
 cudaError_t launch_fluidx(const FluidxArgs &a, const PencilCfg &cfg, int math, cudaStream_t s);
 cudaError_t launch_fluidx_faithful(const FluidxArgs &a, const PencilCfg &cfg, cudaStream_t s);

@@ -22,12 +22,15 @@ static std::map<std::pair<int, int>, PencilCfg> g_tiles;
 static std::atomic<int> g_math{MHD_MATH_FAITHFUL};
 
 // Pencils across memory are staged in rows of PPC cells, so they want many
-// pencils per CTA (a row of 8 cells is 160 bytes of u).
-PencilCfg rows_pick(int n)
+// pencils per CTA (a row of 8 cells is 160 bytes of u).  256-cell pencils take
+// the register-blocked tile with 8 cells per thread (about 150 registers for
+// the fluid update, so fewer pencils per CTA there).
+PencilCfg rows_pick(int kclass, int n)
 {
     if (n <= 32)  return {1, 1, 8};
     if (n <= 64)  return {2, 1, 8};
     if (n <= 128) return {4, 1, 8};
+    if (n == 256) return kclass == MHD_KCLASS_FLUIDX ? PencilCfg{8, 1, 4} : PencilCfg{8, 1, 8};
     if (n <= 256) return {4, 2, 4};
     if (n <= 512) return {4, 4, 2};
     return {4, 8, 1};
@@ -42,7 +45,7 @@ PencilCfg pencil_cfg(int kclass, int n, bool rows)
         auto it = g_tiles.find({tile_key(kclass, rows), n});
         if (it != g_tiles.end()) return it->second;
     }
-    if (rows) return rows_pick(n);
+    if (rows) return rows_pick(kclass, n);
     return kclass == MHD_KCLASS_ADVECT ? advect_pick(n) : fluidx_pick(n);
 }
 

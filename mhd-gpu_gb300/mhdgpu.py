@@ -37,7 +37,8 @@ EXPORTS = [
     "mhdgpu_transpose12", "mhdgpu_transpose13", "mhdgpu_cfl", "mhdgpu_dt_update",
     "mhdgpu_copy_matrix", "mhdgpu_step_workspace_bytes", "mhdgpu_step", "mhdgpu_advance",
     "mhdgpu_step_fused_workspace_bytes", "mhdgpu_step_fused",
-    "mhdgpu_run_host", "mhdgpu_set_math", "mhdgpu_set_tile", "mhdgpu_get_tile",
+    "mhdgpu_run_host", "mhdgpu_resolve_path", "mhdgpu_path_workspace_bytes",
+    "mhdgpu_set_math", "mhdgpu_set_tile", "mhdgpu_get_tile",
     "mhdgpu_autotune", "mhdgpu_profiler_create", "mhdgpu_profiler_destroy",
     "mhdgpu_profiler_attach", "mhdgpu_profiler_reset", "mhdgpu_profiler_summary",
     "mhdgpu_diagnostics_scratch_bytes", "mhdgpu_diagnostics",
@@ -93,6 +94,8 @@ def lib() -> C.CDLL:
             "mhdgpu_step_workspace_bytes": (S, [I, I, I]),
             "mhdgpu_step": (I, [P, P, I, I, I, P, P, P, P]),
             "mhdgpu_step_fused_workspace_bytes": (S, [I, I, I]),
+            "mhdgpu_resolve_path": (I, [I, I, I]),
+            "mhdgpu_path_workspace_bytes": (S, [I, I, I, I]),
             "mhdgpu_step_fused": (I, [P, P, I, I, I, P, P, P, P]),
             "mhdgpu_advance": (I, [P, P, I, I, I, I, D, I, F, P, P, P, I, P]),
             "mhdgpu_run_host": (I, [P, P, I, I, I, D, I, P, F, I, P, P, I]),
@@ -193,12 +196,16 @@ def dt_update(d_inv_c, cfl_number, tf, d_t, d_dt, stream=None):
 
 MHD_PATH_PLAIN = 0
 MHD_PATH_FUSED = 1
+MHD_PATH_AUTO = 2
 
 
 def step_workspace_bytes(nx, ny, nz, path=MHD_PATH_PLAIN) -> int:
-    if path == MHD_PATH_FUSED:
-        return int(lib().mhdgpu_step_fused_workspace_bytes(nx, ny, nz))
-    return int(lib().mhdgpu_step_workspace_bytes(nx, ny, nz))
+    return int(lib().mhdgpu_path_workspace_bytes(nx, ny, nz, int(path)))
+
+
+def resolve_path(nx, ny, nz) -> int:
+    """The path MHD_PATH_AUTO takes for the box (mhdgpu_resolve_path)."""
+    return int(lib().mhdgpu_resolve_path(nx, ny, nz))
 
 
 def step(u, b, nx, ny, nz, d_dt, work, health=None, stream=None):

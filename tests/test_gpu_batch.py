@@ -213,6 +213,27 @@ def test_batch_resume_equals_one_call(gpu):
     _same(got, ref)
 
 
+def test_auto_path_resolves_and_matches(gpu):
+    """MHD_PATH_AUTO takes the transpose-free step for boxes whose y and z
+    pencils are at most 128 cells (or 256), the plain step otherwise, and ends
+    where the path it resolves to ends (the two paths are bit-identical)."""
+    import torch
+    assert gpu.resolve_path(64, 128, 96) == gpu.MHD_PATH_FUSED
+    assert gpu.resolve_path(16, 256, 32) == gpu.MHD_PATH_FUSED
+    assert gpu.resolve_path(16, 8, 200) == gpu.MHD_PATH_PLAIN
+    assert gpu.resolve_path(512, 512, 512) == gpu.MHD_PATH_PLAIN
+    for d in [(24, 16, 20), (8, 4, 160)]:
+        u0, b0 = _states([d], seed=29)[0]
+        runs = []
+        for path in (gpu.MHD_PATH_AUTO, gpu.resolve_path(*d)):
+            du, db = dev(u0), dev(b0)
+            work = torch.empty(gpu.step_workspace_bytes(*d, path), dtype=torch.uint8, device="cuda")
+            clock = gpu.new_clock()
+            gpu.advance(du, db, *d, 3, 0.7, 0, 0.0, clock, None, work, path)
+            runs.append((host(du), host(db), gpu.read_clock(clock)))
+        _same([runs[0]], [runs[1]])
+
+
 def test_batch_run_host_equals_device_path(gpu):
     """mhdgpu_batch_run_host (upload, steps, download, from pinned and from
     pageable host buffers) ends where the device path ends, bit for bit."""
