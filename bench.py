@@ -478,6 +478,42 @@ def ensemble_bench(ens, K, W, stream, flush, world, dev, tune, total_cells):
     return res
 
 
+def large_boxes(stream, dev):
+    """The single-box step at the sizes of the blast and turbulence
+    configurations (256^3 and 512^3) on MHD_PATH_AUTO: the diagonal Alfven
+    wave on the 256^3 box, tiled 2x2x2 on the device for the 512^3 box (still
+    an exact periodic wave; the time per step does not depend on the values),
+    one warm step, then k steps in one advance call timed with CUDA events;
+    the states are larger than L2."""
+    import torch
+    import ics
+    import mhdgpu
+    out = {}
+    u0, b0 = ics.alfven_oblique(256)
+    for n, k in ((256, 10), (512, 5)):
+        r = n // 256
+        du = torch.from_numpy(u0).to(dev).view(256, 256, 256, 5).repeat(r, r, r, 1).reshape(-1)
+        db = torch.from_numpy(b0).to(dev).view(256, 256, 256, 3).repeat(r, r, r, 1).reshape(-1)
+        auto = mhdgpu.MHD_PATH_AUTO
+        work = torch.empty(mhdgpu.step_workspace_bytes(n, n, n, auto), dtype=torch.uint8, device=dev)
+        clock = mhdgpu.new_clock(device=dev)
+        a, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            mhdgpu.advance(du, db, n, n, n, 1, CFL, mhdgpu.MHD_CFL_C, 0.0, clock, None, work, auto, stream=stream)
+            a.record(stream)
+            mhdgpu.advance(du, db, n, n, n, k, CFL, mhdgpu.MHD_CFL_C, 0.0, clock, None, work, auto,
+                           stream=stream, resume=True)
+            e.record(stream)
+        torch.cuda.synchronize()
+        ms = a.elapsed_time(e) / k
+        fused = mhdgpu.resolve_path(n, n, n) == mhdgpu.MHD_PATH_FUSED
+        out[f"{n}^3"] = {"value": n ** 3 / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms, "steps": k,
+                         "path": "MHD_PATH_AUTO -> " + ("transpose-free step" if fused else "plain step"),
+                         "health": mhdgpu.read_clock(clock).health}
+        del du, db, work
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -645,6 +681,8 @@ def main():
             "fused_over_plain": sb["fused_over_plain"],
             "alfven_diag_128": sb, "e2e": sb["e2e"], "clocks": clocks, "health": fused["health"],
         }
+    if world == 1:
+        out["large_boxes"] = large_boxes(stream, dev)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         try:
             if ens_mode:
