@@ -118,7 +118,7 @@ def _spectral_field(r, nx, ny, nz, slope):
     amp = np.zeros_like(kk)
     amp[kk > 0] = kk[kk > 0] ** slope
     noise = np.fft.rfftn(r.standard_normal((nz, ny, nx)))
-    return np.fft.irfftn(noise * amp, s=(nz, ny, nx))
+    return np.fft.irfftn(noise * amp, s=(nz, ny, nx), axes=(0, 1, 2))
 
 
 def turbulence(nx, ny=None, nz=None, seed=0, mach=0.5, b_mean=0.3, db_rms=None, v_rms=None,
