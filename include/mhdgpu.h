@@ -344,14 +344,19 @@ int mhdgpu_batch_read_clocks(mhdgpu_batch *bt, mhdgpu_clock *clocks, mhdgpu_stre
 /* Block schedule of the sweeps along one axis (0, 1, 2): threads per CTA
  * (64, 128 or 256; a CTA holds threads/32 pencils of length <= 128 or half as
  * many longer ones) and resident CTAs per SM (the persistent grid is
- * SMs x ctas_per_sm, capped by the occupancy the kernel allows).  Synchronous
- * (uploads the work tables); not under stream capture. */
+ * SMs x ctas_per_sm, capped by the occupancy the kernel allows).  Synchronous:
+ * waits for the device's queued work, then uploads the work tables; not under
+ * stream capture.  A CUDA graph captured from this handle's steps before a
+ * schedule change (this call or mhdgpu_batch_tune) keeps the old launch shapes
+ * and must be captured again. */
 int mhdgpu_batch_set_schedule(mhdgpu_batch *bt, int axis, int threads, int ctas_per_sm);
 int mhdgpu_batch_get_schedule(const mhdgpu_batch *bt, int axis, int *threads, int *ctas_per_sm);
 /* Autotuner: times every schedule on this batch's own boxes (one warm-up and
  * two timed steps each, CUDA events per sweep), keeps the fastest per axis and
  * restores the boxes' state and clocks.  Allocates a snapshot of the state
- * for the duration; synchronises.  Not under stream capture. */
+ * for the duration; waits for the device's queued work (steps of this handle
+ * already enqueued on any stream finish first); synchronises.  Not under
+ * stream capture. */
 int mhdgpu_batch_tune(mhdgpu_batch *bt, mhdgpu_stream_t stream);
 /* Failure-path test hook: from the next step on, the first dependency wait of
  * box 0 in the first sweep waits for one item more than exist, so it gives up

@@ -222,7 +222,9 @@ void plan_groups(mhdgpu_batch &bt)
 }
 
 // (re)builds the work tables and the launch shapes for the current schedule;
-// synchronous
+// synchronous.  The device tables are read by the class kernels of every step
+// already enqueued, on whatever stream: the upload waits for the device to
+// drain first, so that a step in flight never sees half of a new schedule.
 int build_tables(mhdgpu_batch &bt)
 {
     std::vector<FluidxArgs> &fa = bt.fa;
@@ -302,6 +304,7 @@ int build_tables(mhdgpu_batch &bt)
             g.grid = (int)std::max(1LL, std::min((long long)bt.num_sms * std::min(bt.cps[axis], occ), g.items));
         }
     }
+    BCU(cudaDeviceSynchronize(), "mhdgpu_batch tables");
     BCU(cudaMemcpy(bt.d_start, start.data(), start.size() * sizeof(long long), cudaMemcpyHostToDevice),
         "mhdgpu_batch tables");
     BCU(cudaMemcpy(bt.d_group, group.data(), group.size() * sizeof(int), cudaMemcpyHostToDevice),

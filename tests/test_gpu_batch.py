@@ -140,6 +140,37 @@ def test_batch_tune_restores_state(gpu):
     _same(got, ref)
 
 
+def test_schedule_change_waits_for_steps_in_flight(gpu):
+    """A schedule change (mhdgpu_batch_set_schedule, mhdgpu_batch_tune) issued
+    while steps of the handle still run on a non-blocking stream waits for them
+    before it uploads the new work tables: no dependency wait gives up, and the
+    run ends where one with a synchronisation before each change ends."""
+    import torch
+    dims = [(128, 128, 64), (96, 64, 64), (64, 64, 32), (32, 48, 128)]
+    states = _states(dims, seed=41, amp=0.1)
+    s = torch.cuda.Stream()
+    runs = []
+    for sync in (True, False):
+        boxes = [(dev(u), dev(b), d) for (u, b), d in zip(states, dims)]
+        torch.cuda.synchronize()
+        bt = gpu.Batch(boxes, cfl_number=0.7)
+        bt.advance(6, stream=s)
+        if sync:
+            torch.cuda.synchronize()
+        for axis in range(3):
+            bt.set_schedule(axis, 128, 2)
+        bt.advance(4, stream=s, resume=True)
+        if sync:
+            torch.cuda.synchronize()
+        bt.tune(stream=s)
+        bt.advance(2, stream=s, resume=True)
+        torch.cuda.synchronize()
+        clocks = bt.clocks()            # raises MHD_ERR_TIMEOUT if a wait gave up
+        runs.append([(host(u), host(b), c) for (u, b, _), c in zip(boxes, clocks)])
+        bt.close()
+    _same(runs[1], runs[0])
+
+
 def test_batch_graph_replay(gpu):
     """A captured step replays to the same state as eager steps."""
     import torch
