@@ -569,8 +569,8 @@ def main():
         print(json.dumps({
             "metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": args.gpus, "steps": K,
             "warmup": W, "ms_per_step": ms, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": config, "impl": "reference",
+            "scaling": "strong" if ens_mode else "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "config": config, "impl": "reference",
             "cpu_baseline": {"value": rate, "unit": UNIT, "cores": cores, "kind": kind, "sample": sample},
             "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         }))
