@@ -327,14 +327,19 @@ int mhdgpu_batch_advance(mhdgpu_batch *bt, int nsteps, mhdgpu_stream_t stream);
  * step takes the CFL speeds folded into the previous step's last sweep instead
  * of a reduction pass.  Valid only when no box's state changed since the
  * handle's last advance; the handle runs the pass anyway when it has not
- * advanced yet (or its schedule was tuned since). */
+ * advanced yet (mhdgpu_batch_tune puts the clock records, folded speeds
+ * included, back as they were). */
 int mhdgpu_batch_resume(mhdgpu_batch *bt, int nsteps, mhdgpu_stream_t stream);
 /* The host-buffer entry of the ensemble: uploads every box from h_u[i]
  * (5 floats per cell) and h_b[i] (3 per cell), advances nsteps steps as
  * mhdgpu_batch_advance does, downloads the boxes into the same buffers and
- * synchronises stream.  The copies are spread over the handle's side streams
- * so that several run at once; pinned host buffers copy fastest.  The boxes'
- * device arrays given at creation are overwritten. */
+ * synchronises stream.  With two boxes or more the boxes are split into up to
+ * four parts of about equal cells, pipelined on the handle's side streams:
+ * a part steps as soon as its boxes are uploaded while the next part uploads,
+ * and downloads while later parts still step (the parts are built on the
+ * first call, with the handle's schedule).  Results equal the device path's
+ * bit for bit.  Pinned host buffers copy fastest.  The boxes' device arrays
+ * given at creation are overwritten. */
 int mhdgpu_batch_run_host(mhdgpu_batch *bt, float *const *h_u, float *const *h_b, int nsteps,
                           mhdgpu_stream_t stream);
 /* synchronises stream and copies the nbox clocks to the host; returns

@@ -64,6 +64,9 @@ using namespace mhd;
 namespace {
 
 constexpr int kSweepAxis[6] = {0, 1, 2, 2, 1, 0};
+// parts of mhdgpu_batch_run_host's pipeline (the upload of one part overlaps
+// the steps of the parts before it, their downloads the steps after it)
+constexpr int kHostParts = 4;
 constexpr int kSweepFluidFirst[6] = {1, 1, 1, 0, 0, 0};
 constexpr int kThreadChoices[3] = {64, 128, 256};
 
@@ -111,9 +114,17 @@ struct mhdgpu_batch {
     ClassWork work{};                   // parameter block of one launch (filled per launch)
     cudaStream_t side[kBatchClasses] = {};
     cudaEvent_t fork = nullptr, join[kBatchClasses] = {};
+    std::vector<float> tf_host;         // each box's end time (0: none)
+    // mhdgpu_batch_run_host's pipeline: parts of the boxes (views that share
+    // this handle's states, scratch, clock records and abort word), built on
+    // first use and dropped when the schedule changes
+    std::vector<mhdgpu_batch *> parts;
+    std::vector<std::vector<int>> part_boxes;
+    cudaEvent_t up[kHostParts] = {};
 
     ~mhdgpu_batch()
     {
+        drop_parts();
         cudaFree(d_box); cudaFree(d_clk); cudaFree(d_scr); cudaFree(d_tf);
         cudaFree(d_ctr); cudaFree(d_start); cudaFree(d_group); cudaFree(d_cfl_start);
         for (int i = 0; i < kBatchClasses; ++i) {
@@ -121,6 +132,14 @@ struct mhdgpu_batch {
             if (join[i]) cudaEventDestroy(join[i]);
         }
         if (fork) cudaEventDestroy(fork);
+        for (int i = 0; i < kHostParts; ++i)
+            if (up[i]) cudaEventDestroy(up[i]);
+    }
+    void drop_parts()
+    {
+        for (mhdgpu_batch *p : parts) delete p;
+        parts.clear();
+        part_boxes.clear();
     }
 };
 
@@ -366,6 +385,95 @@ int launch_step(mhdgpu_batch &bt, cudaStream_t s, cudaEvent_t *ev /* 7 events or
     return MHD_OK;
 }
 
+// A part of a handle for the host pipeline: the boxes idx of p with p's
+// states, scratch slices, clock records, end times, schedule and abort word,
+// and its own work tables, counters, streams and events.
+int make_part(const mhdgpu_batch &p, const std::vector<int> &idx, mhdgpu_batch **out)
+{
+    *out = nullptr;
+    const int nbox = (int)idx.size();
+    mhdgpu_batch *bt = new mhdgpu_batch;
+    bt->nbox = nbox;
+    bt->device = p.device;
+    bt->num_sms = p.num_sms;
+    bt->cfl_number = p.cfl_number;
+    bt->cfl_mode = p.cfl_mode;
+    std::copy(p.threads, p.threads + 3, bt->threads);
+    std::copy(p.cps, p.cps + 3, bt->cps);
+    std::vector<long long> cfl_start(nbox + 1);
+    std::vector<float> htf(nbox);
+    for (int j = 0; j < nbox; ++j) {
+        const BoxDesc &d = p.box[idx[j]];
+        bt->box.push_back(d);
+        htf[j] = p.tf_host[idx[j]];
+        cfl_start[j] = bt->cfl_total;
+        bt->cfl_total += batch_chunks((long long)d.nx * d.ny * d.nz, kCflChunk);
+    }
+    cfl_start[nbox] = bt->cfl_total;
+    bt->tf_host = htf;
+    plan_groups(*bt);
+    const size_t ngroups = bt->groups.size();
+    cudaError_t e = cudaMalloc(&bt->d_box, nbox * sizeof(BoxDesc));
+    if (e == cudaSuccess) e = cudaMalloc(&bt->d_tf, nbox * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc(&bt->d_ctr, (bt->nctr + 1) * sizeof(unsigned));
+    if (e == cudaSuccess) e = cudaMalloc(&bt->d_start, (18 * (size_t)nbox + ngroups) * sizeof(long long));
+    if (e == cudaSuccess) e = cudaMalloc(&bt->d_group, 18 * (size_t)nbox * sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&bt->d_cfl_start, (nbox + 1) * sizeof(long long));
+    for (int i = 0; i < kBatchClasses && e == cudaSuccess; ++i) {
+        e = cudaStreamCreateWithFlags(&bt->side[i], cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&bt->join[i], cudaEventDisableTiming);
+    }
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&bt->fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaMemcpy(bt->d_box, bt->box.data(), nbox * sizeof(BoxDesc), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemset(bt->d_ctr, 0, (bt->nctr + 1) * sizeof(unsigned));
+    if (e == cudaSuccess) e = cudaMemcpy(bt->d_tf, htf.data(), nbox * sizeof(float), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(bt->d_cfl_start, cfl_start.data(), (nbox + 1) * sizeof(long long), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        delete bt;
+        return bcuda(e, "mhdgpu_batch_run_host parts");
+    }
+    bt->d_abort = p.d_abort;    // a wait that gives up in a part is the handle's
+    const int st = build_tables(*bt);
+    if (st != MHD_OK) {
+        delete bt;
+        return st;
+    }
+    *out = bt;
+    return MHD_OK;
+}
+
+// Splits the boxes into min(kHostParts, nbox) parts of about equal cells
+// (largest box first, each to the part with the fewest cells).
+int build_parts(mhdgpu_batch &bt)
+{
+    const int np = std::min(kHostParts, bt.nbox);
+    std::vector<int> order(bt.nbox);
+    for (int i = 0; i < bt.nbox; ++i) order[i] = i;
+    auto cells = [&](int i) { return (long long)bt.box[i].nx * bt.box[i].ny * bt.box[i].nz; };
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cells(a) > cells(b); });
+    std::vector<std::vector<int>> part(np);
+    std::vector<long long> load(np, 0);
+    for (int i : order) {
+        const int k = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+        part[k].push_back(i);
+        load[k] += cells(i);
+    }
+    for (int k = 0; k < np; ++k) {
+        std::sort(part[k].begin(), part[k].end());
+        if (!bt.up[k]) BCU(cudaEventCreateWithFlags(&bt.up[k], cudaEventDisableTiming), "mhdgpu_batch_run_host");
+        mhdgpu_batch *q = nullptr;
+        const int st = make_part(bt, part[k], &q);
+        if (st != MHD_OK) {
+            bt.drop_parts();
+            return st;
+        }
+        bt.parts.push_back(q);
+        bt.part_boxes.push_back(part[k]);
+    }
+    return MHD_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -413,6 +521,7 @@ int mhdgpu_batch_create(mhdgpu_batch **out, int nbox, const int *dims, float *co
     cfl_start[nbox] = bt->cfl_total;
     std::vector<float> htf(nbox, 0.0f);
     if (tf) std::copy(tf, tf + nbox, htf.begin());
+    bt->tf_host = htf;
     if (e == cudaSuccess) e = cudaMalloc(&bt->d_box, nbox * sizeof(BoxDesc));
     if (e == cudaSuccess) e = cudaMalloc(&bt->d_clk, nbox * sizeof(mhdgpu_clock));
     if (e == cudaSuccess) e = cudaMalloc(&bt->d_scr, 2 * sizeof(float) * (size_t)cells);
@@ -530,16 +639,60 @@ int mhdgpu_batch_run_host(mhdgpu_batch *bt, float *const *h_u, float *const *h_b
     for (int i = 0; i < bt->nbox; ++i)
         if (!h_u[i] || !h_b[i]) return bfail(MHD_ERR_ARG, "mhdgpu_batch_run_host: null box buffer");
     cudaStream_t s = (cudaStream_t)stream;
-    int st = batch_copy_host(*bt, h_u, h_b, true, s);
-    if (st) return st;
-    // the state was just written from the host: the first step runs the CFL pass
-    for (int it = 0; it < nsteps; ++it) {
-        st = launch_step(*bt, s, nullptr, it == 0);
+    int st = MHD_OK;
+    // the state is written from the host: each part's first step runs the CFL pass
+    bt->folded = false;
+    if (bt->nbox < 2) {
+        st = batch_copy_host(*bt, h_u, h_b, true, s);
         if (st) return st;
-        bt->folded = true;
+        for (int it = 0; it < nsteps; ++it) {
+            st = launch_step(*bt, s, nullptr, it == 0);
+            if (st) return st;
+        }
+        st = batch_copy_host(*bt, h_u, h_b, false, s);
+        if (st) return st;
+    } else {
+        // Pipeline over parts of about equal cells, one stream each: part k
+        // uploads after part k-1 (the host link is the bound), then steps at
+        // once while the later parts upload; its download follows its steps
+        // while the later parts still step.
+        if (bt->parts.empty() && (st = build_parts(*bt)) != MHD_OK) return st;
+        const int np = (int)bt->parts.size();
+        BCU(cudaEventRecord(bt->fork, s), "mhdgpu_batch_run_host fork");
+        for (int k = 0; k < np; ++k) {
+            cudaStream_t cs = bt->side[k];
+            BCU(cudaStreamWaitEvent(cs, bt->fork, 0), "mhdgpu_batch_run_host fork");
+            if (k > 0) BCU(cudaStreamWaitEvent(cs, bt->up[k - 1], 0), "mhdgpu_batch_run_host chain");
+            for (int i : bt->part_boxes[k]) {
+                const BoxDesc &d = bt->box[i];
+                const size_t nc = (size_t)d.nx * d.ny * d.nz;
+                BCU(cudaMemcpyAsync(d.u, h_u[i], 5 * nc * sizeof(float), cudaMemcpyHostToDevice, cs),
+                    "mhdgpu_batch_run_host upload");
+                BCU(cudaMemcpyAsync(d.b, h_b[i], 3 * nc * sizeof(float), cudaMemcpyHostToDevice, cs),
+                    "mhdgpu_batch_run_host upload");
+            }
+            BCU(cudaEventRecord(bt->up[k], cs), "mhdgpu_batch_run_host chain");
+            for (int it = 0; it < nsteps; ++it)
+                if ((st = launch_step(*bt->parts[k], cs, nullptr, it == 0)) != MHD_OK) return st;
+        }
+        // downloads are issued after every part's steps: a copy into pageable
+        // memory returns only when done, and must not hold back later parts
+        for (int k = 0; k < np; ++k) {
+            cudaStream_t cs = bt->side[k];
+            for (int i : bt->part_boxes[k]) {
+                const BoxDesc &d = bt->box[i];
+                const size_t nc = (size_t)d.nx * d.ny * d.nz;
+                BCU(cudaMemcpyAsync(h_u[i], d.u, 5 * nc * sizeof(float), cudaMemcpyDeviceToHost, cs),
+                    "mhdgpu_batch_run_host download");
+                BCU(cudaMemcpyAsync(h_b[i], d.b, 3 * nc * sizeof(float), cudaMemcpyDeviceToHost, cs),
+                    "mhdgpu_batch_run_host download");
+            }
+            BCU(cudaEventRecord(bt->join[k], cs), "mhdgpu_batch_run_host join");
+            BCU(cudaStreamWaitEvent(s, bt->join[k], 0), "mhdgpu_batch_run_host join");
+        }
     }
-    st = batch_copy_host(*bt, h_u, h_b, false, s);
-    if (st) return st;
+    // the clocks now hold the last step's folded CFL speeds
+    bt->folded = nsteps > 0;
     BCU(cudaStreamSynchronize(s), "mhdgpu_batch_run_host");
     return MHD_OK;
 }
@@ -572,6 +725,7 @@ int mhdgpu_batch_set_schedule(mhdgpu_batch *bt, int axis, int threads, int ctas_
     const int old_t = bt->threads[axis], old_c = bt->cps[axis];
     bt->threads[axis] = threads;
     bt->cps[axis] = ctas_per_sm;
+    bt->drop_parts();
     const int st = build_tables(*bt);
     if (st != MHD_OK) {
         bt->threads[axis] = old_t;
@@ -664,6 +818,7 @@ int mhdgpu_batch_tune(mhdgpu_batch *bt, mhdgpu_stream_t stream)
         bt->threads[a] = st == MHD_OK ? best_t[a] : keep_t[a];
         bt->cps[a] = st == MHD_OK ? best_c[a] : keep_c[a];
     }
+    bt->drop_parts();
     const int st2 = build_tables(*bt);
     // restore the state, the clocks and the counters
     off = 0;

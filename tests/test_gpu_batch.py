@@ -288,6 +288,42 @@ def test_batch_run_host_equals_device_path(gpu):
         _same(got, ref)
 
 
+def test_batch_run_host_pipeline_resume_and_reschedule(gpu):
+    """The host entry's pipeline over parts leaves the folded CFL speeds in
+    the handle's clocks (a resumed device step continues it), rebuilds its
+    parts after a schedule change, and a single-box handle takes the direct
+    path; every run ends where the device path ends, bit for bit."""
+    import torch
+    dims = CLASS_BOXES[:7]
+    states = _states(dims, seed=31)
+    ref = _batched(gpu, states, dims, 4, 0.7)
+    boxes = [(dev(np.zeros_like(u)), dev(np.zeros_like(b)), d) for (u, b), d in zip(states, dims)]
+    bt = gpu.Batch(boxes, cfl_number=0.7)
+    hu = [torch.from_numpy(u.copy()).pin_memory() for u, _ in states]
+    hb = [torch.from_numpy(b.copy()).pin_memory() for _, b in states]
+    bt.run_host(hu, hb, 2)
+    bt.advance(1, resume=True)
+    for axis in range(3):
+        bt.set_schedule(axis, 128, 4)
+    hu = [u.cpu().pin_memory() for u, _, _ in boxes]
+    hb = [b.cpu().pin_memory() for _, b, _ in boxes]
+    bt.run_host(hu, hb, 1)
+    clocks = bt.clocks()
+    got = [(x.numpy(), y.numpy(), c) for x, y, c in zip(hu, hb, clocks)]
+    bt.close()
+    _same(got, ref)
+    one = [dims[1]]
+    ref1 = _batched(gpu, states[1:2], one, 2, 0.7)
+    box1 = [(dev(np.zeros_like(states[1][0])), dev(np.zeros_like(states[1][1])), one[0])]
+    b1 = gpu.Batch(box1, cfl_number=0.7)
+    hu1 = [torch.from_numpy(states[1][0].copy())]
+    hb1 = [torch.from_numpy(states[1][1].copy())]
+    b1.run_host(hu1, hb1, 2)
+    got1 = [(hu1[0].numpy(), hb1[0].numpy(), b1.clocks()[0])]
+    b1.close()
+    _same(got1, ref1)
+
+
 def test_batch_fast_math_matches_per_box(gpu):
     """The fast policy lets the compiler contract multiply-adds, and the
     contraction can differ between the single-box and the batched kernels in
