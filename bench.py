@@ -473,7 +473,8 @@ def ensemble_bench(ens, K, W, stream, flush, world, dev, tune, total_cells):
     res["e2e"] = {"value": total_cells * ke / s3, "unit": UNIT, "steps": ke,
                   "h2d_bytes_per_step": 32 * cells, "d2h_bytes_per_step": 32 * cells,
                   "api": "mhdgpu_batch_run_host (1 step per call): pinned host -> device copies of every "
-                         "box, the batched step, device -> host copies, synchronised"}
+                         "box, the batched step, device -> host copies, synchronised; the library "
+                         "pipelines four parts of the boxes (a part's copies overlap the other parts' steps)"}
     bt.close()
     return res
 
