@@ -209,13 +209,17 @@ int mhdgpu_advance(float *u, float *b, int nx, int ny, int nz, int nsteps,
 /* ------------------------------------------------------------------------
  * Host-buffer entry (the end-to-end path): uploads (u, b) from host memory,
  * runs up to max_steps steps as mhdgpu_advance does, downloads the state.
- * Allocates its device buffers per call.  *t is read and updated; dt_log may
+ * Its device buffers and stream are kept per host thread between calls
+ * (grown to the largest box seen; mhdgpu_release_host_cache frees them, and
+ * they are freed when the thread ends).  *t is read and updated; dt_log may
  * be NULL.  Returns the steps taken in *steps_done (may be NULL).  path as
  * for mhdgpu_advance.
  * ------------------------------------------------------------------------ */
 int mhdgpu_run_host(float *u, float *b, int nx, int ny, int nz, double cfl_number,
                     int cfl_mode, float *t, float tf, int max_steps, float *dt_log,
                     int *steps_done, int path);
+/* Frees the calling thread's device buffers and stream of mhdgpu_run_host. */
+int mhdgpu_release_host_cache(void);
 
 /* ------------------------------------------------------------------------
  * Arithmetic policy and tile shapes (process-wide settings, host side).

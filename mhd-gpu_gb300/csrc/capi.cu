@@ -356,6 +356,31 @@ int mhdgpu_advance(float *u, float *b, int nx, int ny, int nz, int nsteps, doubl
     return MHD_OK;
 }
 
+// The host-buffer entry's device memory and stream, kept per host thread
+// between calls (allocating and mapping ~40 B/cell per call cost about a
+// third of a 128^3 call); grown to the largest request, released by
+// mhdgpu_release_host_cache or when the thread ends.
+struct HostEntryCache {
+    int device = -1;
+    cudaStream_t s = nullptr;
+    char *buf = nullptr;
+    size_t cap = 0;
+    void release()
+    {
+        if (s) cudaStreamSynchronize(s);
+        if (buf) cudaFree(buf);
+        if (s) cudaStreamDestroy(s);
+        buf = nullptr;
+        cap = 0;
+        s = nullptr;
+        device = -1;
+    }
+    ~HostEntryCache() { release(); }
+};
+static thread_local HostEntryCache g_host_cache;
+
+static size_t align256(size_t n) { return (n + 255) & ~(size_t)255; }
+
 int mhdgpu_run_host(float *u, float *b, int nx, int ny, int nz, double cfl_number, int cfl_mode,
                     float *t, float tf, int max_steps, float *dt_log, int *steps_done, int path)
 {
@@ -370,19 +395,40 @@ int mhdgpu_run_host(float *u, float *b, int nx, int ny, int nz, double cfl_numbe
     const size_t wbytes = path == MHD_PATH_FUSED ? mhdgpu_step_fused_workspace_bytes(nx, ny, nz)
                                                  : mhdgpu_step_workspace_bytes(nx, ny, nz);
     if (!wbytes) return fail(MHD_ERR_ARG, "mhdgpu_run_host: box too large for the step");
-    float *du = nullptr, *db = nullptr, *dlog = nullptr;
-    void *dw = nullptr;
-    mhdgpu_clock *dclk = nullptr;
-    cudaStream_t s = nullptr;
+    // carve u, b, workspace, clock and dt log out of the thread's buffer
+    const size_t o_b = align256(ncell * 5 * sizeof(float));
+    const size_t o_w = o_b + align256(ncell * 3 * sizeof(float));
+    const size_t o_c = o_w + align256(wbytes);
+    const size_t o_l = o_c + align256(sizeof(mhdgpu_clock));
+    const size_t need = o_l + align256(sizeof(float) * (max_steps > 0 ? max_steps : 1));
+    HostEntryCache &hc = g_host_cache;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return cuda_fail(e, "mhdgpu_run_host: device");
+    if (hc.device != dev) {
+        hc.release();
+        if ((e = cudaStreamCreateWithFlags(&hc.s, cudaStreamNonBlocking)) != cudaSuccess) {
+            hc.s = nullptr;
+            return cuda_fail(e, "mhdgpu_run_host: stream");
+        }
+        hc.device = dev;
+    }
+    if (hc.cap < need) {
+        if (hc.buf) cudaFree(hc.buf);
+        hc.buf = nullptr;
+        hc.cap = 0;
+        if ((e = cudaMalloc((void **)&hc.buf, need)) != cudaSuccess) {
+            hc.buf = nullptr;
+            return cuda_fail(e, "mhdgpu_run_host: alloc");
+        }
+        hc.cap = need;
+    }
+    cudaStream_t s = hc.s;
+    float *du = (float *)hc.buf, *db = (float *)(hc.buf + o_b), *dlog = (float *)(hc.buf + o_l);
+    void *dw = hc.buf + o_w;
+    mhdgpu_clock *dclk = (mhdgpu_clock *)(hc.buf + o_c);
     int ret = MHD_OK;
-    cudaError_t e;
 #define RH(call, where) do { e = (call); if (e != cudaSuccess) { ret = cuda_fail(e, where); goto done; } } while (0)
-    RH(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), "mhdgpu_run_host: stream");
-    RH(cudaMallocAsync((void **)&du, ncell * 5 * sizeof(float), s), "mhdgpu_run_host: alloc");
-    RH(cudaMallocAsync((void **)&db, ncell * 3 * sizeof(float), s), "mhdgpu_run_host: alloc");
-    RH(cudaMallocAsync(&dw, wbytes, s), "mhdgpu_run_host: alloc");
-    RH(cudaMallocAsync((void **)&dclk, sizeof(mhdgpu_clock), s), "mhdgpu_run_host: alloc");
-    RH(cudaMallocAsync((void **)&dlog, sizeof(float) * (max_steps > 0 ? max_steps : 1), s), "mhdgpu_run_host: alloc");
     {
         mhdgpu_clock h;
         memset(&h, 0, sizeof h);
@@ -405,17 +451,16 @@ int mhdgpu_run_host(float *u, float *b, int nx, int ny, int nz, double cfl_numbe
             ret = fail(MHD_ERR_UNPHYSICAL, "mhdgpu_run_host: health word reports NaN/Inf or rho <= 0");
     }
 done:
-    if (s) {
-        cudaFreeAsync(du, s);
-        cudaFreeAsync(db, s);
-        cudaFreeAsync(dw, s);
-        cudaFreeAsync(dclk, s);
-        cudaFreeAsync(dlog, s);
-        cudaStreamSynchronize(s);
-        cudaStreamDestroy(s);
-    }
+    // nothing of this call may still run on the stream when it returns
+    if (ret != MHD_OK) cudaStreamSynchronize(s);
 #undef RH
     return ret;
+}
+
+int mhdgpu_release_host_cache(void)
+{
+    g_host_cache.release();
+    return MHD_OK;
 }
 
 }  // extern "C"

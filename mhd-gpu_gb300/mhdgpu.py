@@ -37,7 +37,7 @@ EXPORTS = [
     "mhdgpu_transpose12", "mhdgpu_transpose13", "mhdgpu_cfl", "mhdgpu_dt_update",
     "mhdgpu_copy_matrix", "mhdgpu_step_workspace_bytes", "mhdgpu_step", "mhdgpu_advance",
     "mhdgpu_step_fused_workspace_bytes", "mhdgpu_step_fused",
-    "mhdgpu_run_host", "mhdgpu_resolve_path", "mhdgpu_path_workspace_bytes",
+    "mhdgpu_run_host", "mhdgpu_release_host_cache", "mhdgpu_resolve_path", "mhdgpu_path_workspace_bytes",
     "mhdgpu_set_math", "mhdgpu_set_tile", "mhdgpu_get_tile",
     "mhdgpu_autotune", "mhdgpu_profiler_create", "mhdgpu_profiler_destroy",
     "mhdgpu_profiler_attach", "mhdgpu_profiler_reset", "mhdgpu_profiler_summary",
@@ -99,6 +99,7 @@ def lib() -> C.CDLL:
             "mhdgpu_step_fused": (I, [P, P, I, I, I, P, P, P, P]),
             "mhdgpu_advance": (I, [P, P, I, I, I, I, D, I, F, P, P, P, I, P]),
             "mhdgpu_run_host": (I, [P, P, I, I, I, D, I, P, F, I, P, P, I]),
+            "mhdgpu_release_host_cache": (I, []),
             "mhdgpu_set_math": (I, [I]),
             "mhdgpu_set_tile": (I, [I, I, I, I, I]),
             "mhdgpu_get_tile": (I, [I, I, P, P, P]),
@@ -259,6 +260,11 @@ def run_host(u, b, nx, ny, nz, cfl_number=0.9, cfl_mode=MHD_CFL_C, t=0.0, tf=0.0
     if st not in (MHD_OK, MHD_ERR_UNPHYSICAL):
         _check(st)
     return st, tt.value, done.value
+
+
+def release_host_cache():
+    """Frees this thread's device buffers and stream kept by run_host."""
+    _check(lib().mhdgpu_release_host_cache())
 
 
 MHD_MATH_FAITHFUL = 0

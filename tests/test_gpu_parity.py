@@ -306,6 +306,27 @@ def test_run_host_matches_device_path(gpu, path):
     assert bits_equal(hu, gu) and bits_equal(hb, gb) and bits_equal(log, dts)
 
 
+def test_run_host_cache_grows_and_releases(gpu):
+    """The host entry keeps its device buffers per thread: a small box, a
+    larger one (the buffer grows), the small one again inside the larger
+    buffer, and a call after mhdgpu_release_host_cache all equal the device
+    path bit for bit."""
+    import ics
+    cases = [((16, 16, 16), ics.alfven_x(16)), ((24, 16, 32), ics.random_state(24, 16, 32, seed=9, amp=0.1))]
+    refs = {}
+    for dims, (u, b) in cases:
+        gu, gb, _dts, _clk = _advance(gpu, u, b, *dims, 3, 0.7, path=gpu.MHD_PATH_FUSED)
+        refs[dims] = (gu, gb)
+    for k, release in ((0, False), (1, False), (0, False), (1, True), (0, True)):
+        dims, (u, b) = cases[k]
+        if release:
+            gpu.release_host_cache()
+        hu, hb = u.copy(), b.copy()
+        st, _t, done = gpu.run_host(hu, hb, *dims, 0.7, 0, 0.0, 0.0, 3, path=gpu.MHD_PATH_FUSED)
+        assert st == gpu.MHD_OK and done == 3
+        assert bits_equal(hu, refs[dims][0]) and bits_equal(hb, refs[dims][1])
+
+
 def test_health_word_flags_unphysical_state(gpu):
     """Fault injection on the host: a negative density uploaded into the
     state.  The kernels keep running; the health word reports it."""
