@@ -14,7 +14,10 @@
 // outer axis o.  Rows of 32 cells (160 floats of u, 96 of b) are read and
 // written with consecutive threads on consecutive addresses; the tile rows in
 // shared memory are padded to a stride of 5 (u) or 3 (b) banks mod 32 so the
-// transposed read is conflict-free.
+// transposed read is conflict-free.  A full tile whose rows start on 16-byte
+// boundaries (the strides along b and o multiples of 4 cells, 16-byte aligned
+// arrays) moves 16-byte vectors, all of a thread's loads issued before its
+// shared-memory stores; other tiles move single floats.
 #include "kernels.cuh"
 
 namespace mhd {
@@ -27,6 +30,7 @@ struct TransposeArgs {
     long long sa_out, so_out;    // destination cell strides of a and o (b has stride 1)
     unsigned pu, pb;             // destination component ii <- source component
                                  // (p >> 4*ii) & 15 (packed so no local array)
+    int vec;                     // full tiles may move 16-byte vectors
 };
 
 constexpr int kTile = 32;
@@ -43,6 +47,64 @@ transpose_kernel(TransposeArgs t)
     const long long o = blockIdx.z;
     const int na = min(kTile, t.A - a0);
     const int nb = min(kTile, t.B - b0);
+
+    if (t.vec && na == kTile && nb == kTile) {
+        // u: 32 rows x 40 vectors, b: 32 rows x 24 vectors; 256 threads
+        constexpr int kVu = kTile * kTile * 5 / 4 / 256, kVb = kTile * kTile * 3 / 4 / 256;
+        float4 lu[kVu], lb[kVb];
+#pragma unroll
+        for (int k = 0; k < kVu; ++k) {
+            const int e = threadIdx.x + 256 * k, r = e / 40, c = e - r * 40;
+            const long long cell = (long long)a0 + (long long)(b0 + r) * t.sb_in + o * t.so_in;
+            lu[k] = __ldg(reinterpret_cast<const float4 *>(t.su + cell * 5) + c);
+        }
+#pragma unroll
+        for (int k = 0; k < kVb; ++k) {
+            const int e = threadIdx.x + 256 * k, r = e / 24, c = e - r * 24;
+            const long long cell = (long long)a0 + (long long)(b0 + r) * t.sb_in + o * t.so_in;
+            lb[k] = __ldg(reinterpret_cast<const float4 *>(t.sb + cell * 3) + c);
+        }
+#pragma unroll
+        for (int k = 0; k < kVu; ++k) {
+            const int e = threadIdx.x + 256 * k, r = e / 40, c = e - r * 40;
+            float *d = tu + r * kRowU + 4 * c;
+            d[0] = lu[k].x; d[1] = lu[k].y; d[2] = lu[k].z; d[3] = lu[k].w;
+        }
+#pragma unroll
+        for (int k = 0; k < kVb; ++k) {
+            const int e = threadIdx.x + 256 * k, r = e / 24, c = e - r * 24;
+            float *d = tb + r * kRowB + 4 * c;
+            d[0] = lb[k].x; d[1] = lb[k].y; d[2] = lb[k].z; d[3] = lb[k].w;
+        }
+        __syncthreads();
+        // destination row s: floats 4c .. 4c+3 of the row are (cell, component)
+        // pairs (col / 5, col % 5) of u, (col / 3, col % 3) of b
+#pragma unroll
+        for (int k = 0; k < kVu; ++k) {
+            const int e = threadIdx.x + 256 * k, s = e / 40, c = e - s * 40;
+            float v[4];
+#pragma unroll
+            for (int m = 0; m < 4; ++m) {
+                const int col = 4 * c + m, bb = col / 5, cc = col - bb * 5;
+                v[m] = tu[bb * kRowU + s * 5 + ((t.pu >> (4 * cc)) & 15u)];
+            }
+            const long long cell = (long long)b0 + (long long)(a0 + s) * t.sa_out + o * t.so_out;
+            reinterpret_cast<float4 *>(t.du + cell * 5)[c] = make_float4(v[0], v[1], v[2], v[3]);
+        }
+#pragma unroll
+        for (int k = 0; k < kVb; ++k) {
+            const int e = threadIdx.x + 256 * k, s = e / 24, c = e - s * 24;
+            float v[4];
+#pragma unroll
+            for (int m = 0; m < 4; ++m) {
+                const int col = 4 * c + m, bb = col / 3, cc = col - bb * 3;
+                v[m] = tb[bb * kRowB + s * 3 + ((t.pb >> (4 * cc)) & 15u)];
+            }
+            const long long cell = (long long)b0 + (long long)(a0 + s) * t.sa_out + o * t.so_out;
+            reinterpret_cast<float4 *>(t.db + cell * 3)[c] = make_float4(v[0], v[1], v[2], v[3]);
+        }
+        return;
+    }
 
     // load: tile row r = source row b0+r, 32 cells along a
     for (int e = threadIdx.x; e < kTile * kTile * 5; e += blockDim.x) {
@@ -99,6 +161,12 @@ cudaError_t launch_transpose(float *du, float *db, const float *su, const float 
         t.pu = 0x41230u;   // (0, 3, 2, 1, 4)
         t.pb = 0x012u;     // (2, 1, 0)
     }
+    // 16-byte rows: a row starts at cell a0 + b*sb_in + o*so_in (a0 a multiple
+    // of 32), i.e. at byte 20 cell (u) or 12 cell (b), aligned when the cell
+    // index is a multiple of 4; likewise for the destination rows
+    auto al16 = [](const void *p) { return ((unsigned long long)p & 15ull) == 0; };
+    t.vec = t.sb_in % 4 == 0 && t.so_in % 4 == 0 && t.sa_out % 4 == 0 && t.so_out % 4 == 0 &&
+            al16(du) && al16(db) && al16(su) && al16(sb);
     if (t.O > 65535) return cudaErrorInvalidConfiguration;
     dim3 grid((t.A + kTile - 1) / kTile, (t.B + kTile - 1) / kTile, t.O);
     transpose_kernel<<<grid, 256, 0, s>>>(t);

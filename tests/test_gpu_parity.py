@@ -78,7 +78,10 @@ def test_advectbyzx_matches_oracle(gpu, oracle_lib, dims):
 
 
 @pytest.mark.parametrize("dims", [(16, 16, 16), (8, 6, 10), (5, 7, 9), (33, 31, 2), (64, 1, 40),
-                                  (1, 1, 1), (7, 70, 3)])
+                                  (1, 1, 1), (7, 70, 3),
+                                  # full 32x32 tiles on 16-byte rows (vector copies), with
+                                  # ragged edge tiles beside them, and unaligned strides
+                                  (64, 96, 32), (96, 40, 68), (64, 36, 44), (32, 64, 30), (36, 64, 64)])
 def test_transposes_bit_exact(gpu, oracle_lib, dims):
     import ics
     O = oracle_lib.oracle("f32")
