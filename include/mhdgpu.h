@@ -165,11 +165,12 @@ int mhdgpu_step_fused(float *u, float *b, int nx, int ny, int nz, const float *d
 #define MHD_PATH_AUTO       2   /* the faster of the two for the box (mhdgpu_resolve_path) */
 
 /* The path MHD_PATH_AUTO takes for an nx*ny*nz box: MHD_PATH_FUSED when
- * every y and z pencil has at most 128 cells or exactly 256 (their sweeps
- * stage whole rows of pencils efficiently), else MHD_PATH_PLAIN (measured on
- * GB300: at 512^3 the plain step is 1.6x faster, at 128^3 the transpose-free
- * one 1.15x).  mhdgpu_path_workspace_bytes sizes the workspace of a path
- * (MHD_PATH_AUTO: of the path it takes). */
+ * every y and z pencil has at most 128 cells, else MHD_PATH_PLAIN (measured
+ * on GB300: the transpose-free step is 1.27x faster at 32^3 and even with
+ * the plain one at 64^3-128^3; the plain step, whose transposes run near the
+ * copy bandwidth, is 1.09x faster at 256^3 and 1.71x at 512^3).
+ * mhdgpu_path_workspace_bytes sizes the workspace of a path (MHD_PATH_AUTO:
+ * of the path it takes). */
 int mhdgpu_resolve_path(int nx, int ny, int nz);
 size_t mhdgpu_path_workspace_bytes(int nx, int ny, int nz, int path);
 

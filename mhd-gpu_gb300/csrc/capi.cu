@@ -308,8 +308,7 @@ static int step_fused(float *u, float *b, int nx, int ny, int nz, const float *d
 
 int mhdgpu_resolve_path(int nx, int ny, int nz)
 {
-    auto staged = [](int n) { return n <= 128 || n == 256; };
-    return (staged(ny) && staged(nz)) ? MHD_PATH_FUSED : MHD_PATH_PLAIN;
+    return (ny <= 128 && nz <= 128) ? MHD_PATH_FUSED : MHD_PATH_PLAIN;
 }
 
 size_t mhdgpu_path_workspace_bytes(int nx, int ny, int nz, int path)
