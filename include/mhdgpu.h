@@ -219,7 +219,8 @@ int mhdgpu_advance(float *u, float *b, int nx, int ny, int nz, int nsteps,
 int mhdgpu_run_host(float *u, float *b, int nx, int ny, int nz, double cfl_number,
                     int cfl_mode, float *t, float tf, int max_steps, float *dt_log,
                     int *steps_done, int path);
-/* Frees the calling thread's device buffers and stream of mhdgpu_run_host. */
+/* Frees the calling thread's device buffers and stream of mhdgpu_run_host
+ * (call it before resetting the device from that thread). */
 int mhdgpu_release_host_cache(void);
 
 /* ------------------------------------------------------------------------
