@@ -359,7 +359,8 @@ def single_box(n, K, W, stream, flush, world, dev, tune, math_mode):
             res["fluidx_roofline"] = {
                 "bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
                 "peak_source": f"{kind} (MEASURED_PEAKS.json hbm_gbs)",
-                "traffic": read_traffic("fluidx_alfven128_ncu.txt"),
+                # the committed capture is of the 128^3 launch
+                "traffic": read_traffic("fluidx_alfven128_ncu.txt") if n == 128 else None,
                 "algorithmic_bytes_per_launch": FLUIDX_BYTES_PER_CELL * ncell,
                 "avg_launch_us": fl_avg_s * 1e6, "share_of_step": fl_ms / tot_ms if tot_ms else None}
     res["fused_over_plain"] = res["fused"]["value"] / res["plain"]["value"]
@@ -661,7 +662,7 @@ def main():
                               "path": eb["boxwise_plain"]["path"]},
             "fused_over_plain": eb["batched_over_boxwise_plain"],
             "ensemble": {k: v for k, v in eb.items() if k not in ("roofline", "wall", "e2e")},
-            "alfven_diag_128": sb,
+            sb["workload"]: sb,
             "e2e": eb["e2e"], "clocks": clocks, "health": eb["health"],
         }
     else:
@@ -680,7 +681,7 @@ def main():
             "plain_drop_in": {"value": sb["plain"]["value"], "unit": UNIT,
                               "ms_per_step": sb["plain"]["ms_per_step"], "path": sb["plain"]["path"]},
             "fused_over_plain": sb["fused_over_plain"],
-            "alfven_diag_128": sb, "e2e": sb["e2e"], "clocks": clocks, "health": fused["health"],
+            sb["workload"]: sb, "e2e": sb["e2e"], "clocks": clocks, "health": fused["health"],
         }
     if world == 1:
         out["large_boxes"] = large_boxes(stream, dev)
