@@ -47,6 +47,14 @@ batch_cfl_kernel(CflWork w)
     }
 }
 
+// Each box's CFL word cleared before a reduction pass: the state may have
+// changed since the last step folded its speed into the word.
+__global__ void batch_cmax_clear_kernel(const BoxDesc *box, int nbox)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < nbox) box[i].clk->cmax = 0u;
+}
+
 // One clock tick per box, and the sweeps' claim and completion counters
 // cleared for the step.
 __global__ void batch_clock_kernel(const BoxDesc *box, const float *tf, int nbox, double cfl_number,
@@ -342,15 +350,17 @@ int build_tables(mhdgpu_batch &bt)
     return MHD_OK;
 }
 
-// One step.  With first set the CFL reduction runs as its own pass; otherwise
-// the previous step's last sweep has folded it into the clock words (a max,
-// so a pass over the same state changes nothing).
+// One step.  With first set the CFL reduction runs as its own pass (on
+// cleared words); otherwise the previous step's last sweep has folded it into
+// the clock words.
 int launch_step(mhdgpu_batch &bt, cudaStream_t s, cudaEvent_t *ev /* 7 events or NULL */, bool first)
 {
     const int nb = bt.nbox;
     {
-        ProfScope ps(MHD_KCLASS_CFL, first ? 2 : 1, s);
+        ProfScope ps(MHD_KCLASS_CFL, first ? 3 : 1, s);
         if (first) {
+            batch_cmax_clear_kernel<<<(nb + 255) / 256, 256, 0, s>>>(bt.d_box, nb);
+            BCU(cudaGetLastError(), "mhdgpu_batch_advance cfl");
             CflWork cw{bt.d_box, bt.d_cfl_start, nb, bt.cfl_mode};
             const int g = (int)std::max(1LL, std::min((long long)bt.num_sms * 8, bt.cfl_total));
             batch_cfl_kernel<<<g, kCflThreads, 0, s>>>(cw);

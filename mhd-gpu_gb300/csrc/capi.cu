@@ -336,13 +336,16 @@ int mhdgpu_advance(float *u, float *b, int nx, int ny, int nz, int nsteps, doubl
     cudaStream_t s = (cudaStream_t)stream;
     // The CFL reduction runs as its own pass before the first step of the
     // call (unless the caller resumes); every step's last fluid sweep folds
-    // the next step's reduction into the clock's word (a max, so the first
-    // pass of a later call, over the same state, changes nothing).
+    // the next step's reduction into the clock's word.  The pass clears the
+    // word first: the state may have changed since a previous call's fold.
     for (int it = 0; it < nsteps; ++it) {
         const bool pass = it == 0 && !resume;
         {
             ProfScope ps(MHD_KCLASS_CFL, pass ? 2 : 1, s);
-            if (pass) MHD_CU(launch_cfl(u, b, nx, ny, nz, cfl_mode, &d_clock->cmax, s), "mhdgpu_advance");
+            if (pass) {
+                MHD_CU(cudaMemsetAsync(&d_clock->cmax, 0, sizeof(unsigned), s), "mhdgpu_advance");
+                MHD_CU(launch_cfl(u, b, nx, ny, nz, cfl_mode, &d_clock->cmax, s), "mhdgpu_advance");
+            }
             MHD_CU(launch_clock(d_clock, cfl_number, tf, d_dt_log, s), "mhdgpu_advance");
         }
         int st = (path == MHD_PATH_FUSED)

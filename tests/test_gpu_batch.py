@@ -226,6 +226,55 @@ def test_advance_resume_equals_one_call(gpu, path):
     assert runs[1][2].iter == 4
 
 
+@pytest.mark.parametrize("path", [0, 1])
+def test_new_state_after_steps_takes_its_own_cfl(gpu, path):
+    """A step's last sweep folds the next CFL speed into the clock; a later
+    call without resume on a state written in between (a slower one here)
+    must take that state's own speed, as a fresh clock does: single box and
+    batch (device and host-buffer entries)."""
+    import torch
+    d = (32, 24, 16)
+    fast = _states([d], seed=3, amp=0.6)[0]
+    slow = _states([d], seed=4, amp=0.01)[0]
+    work = torch.empty(gpu.step_workspace_bytes(*d, path), dtype=torch.uint8, device="cuda")
+    ref_u, ref_b = dev(slow[0]), dev(slow[1])
+    ref_clk = gpu.new_clock()
+    gpu.advance(ref_u, ref_b, *d, 1, 0.7, 0, 0.0, ref_clk, None, work, path)
+    ref = gpu.read_clock(ref_clk)
+    du, db = dev(fast[0]), dev(fast[1])
+    clk = gpu.new_clock()
+    gpu.advance(du, db, *d, 2, 0.7, 0, 0.0, clk, None, work, path)
+    du.copy_(dev(slow[0]))
+    db.copy_(dev(slow[1]))
+    t0 = gpu.read_clock(clk).t
+    gpu.advance(du, db, *d, 1, 0.7, 0, 0.0, clk, None, work, path)
+    c = gpu.read_clock(clk)
+    assert c.dt == ref.dt and c.t == np.float32(np.float32(t0) + np.float32(2) * np.float32(ref.dt))
+    assert bits_equal(host(du), host(ref_u)) and bits_equal(host(db), host(ref_b))
+    if path:
+        return
+    dims = [d, (16, 40, 8)]
+    fasts = _states(dims, seed=7, amp=0.6)
+    slows = _states(dims, seed=8, amp=0.01)
+    ref_batch = _batched(gpu, slows, dims, 1, 0.7)
+    boxes = [(dev(u), dev(b), dd) for (u, b), dd in zip(fasts, dims)]
+    bt = gpu.Batch(boxes, cfl_number=0.7)
+    bt.advance(2)
+    for (u, b, _), (su, sb) in zip(boxes, slows):
+        u.copy_(dev(su))
+        b.copy_(dev(sb))
+    bt.advance(1)
+    got = [(host(u), host(b), c) for (u, b, _), c in zip(boxes, bt.clocks())]
+    assert [g[2].dt for g in got] == [r[2].dt for r in ref_batch]
+    assert all(bits_equal(g[0], r[0]) and bits_equal(g[1], r[1]) for g, r in zip(got, ref_batch))
+    hu = [torch.from_numpy(u.copy()).pin_memory() for u, _ in slows]
+    hb = [torch.from_numpy(b.copy()).pin_memory() for _, b in slows]
+    bt.run_host(hu, hb, 1)               # a host state written over the stepped one
+    got = [c.dt for c in bt.clocks()]
+    assert got == [r[2].dt for r in ref_batch]
+    bt.close()
+
+
 def test_batch_resume_equals_one_call(gpu):
     """mhdgpu_batch_resume continues without the CFL pass and ends where one
     multi-step mhdgpu_batch_advance ends; on a handle that has not advanced
