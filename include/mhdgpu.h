@@ -195,7 +195,8 @@ typedef struct {
  * mhdgpu_step_fused_workspace_bytes).
  *
  * The CFL reduction runs as its own pass over the state before the call's
- * first step; each step's last fluid sweep folds the next step's reduction
+ * first step (on a cleared word, so a state written since the clock's last
+ * step takes its own speed); each step's last fluid sweep folds the next step's reduction
  * into the clock's CFL word, so later steps of the call need no pass.  With
  * MHD_ADVANCE_RESUME or'ed into cfl_mode, the first step takes that folded
  * word too: valid only when the clock's last step was taken by mhdgpu_advance
