@@ -364,7 +364,7 @@ int mhdgpu_batch_read_clocks(mhdgpu_batch *bt, mhdgpu_clock *clocks, mhdgpu_stre
 int mhdgpu_batch_set_schedule(mhdgpu_batch *bt, int axis, int threads, int ctas_per_sm);
 int mhdgpu_batch_get_schedule(const mhdgpu_batch *bt, int axis, int *threads, int *ctas_per_sm);
 /* Autotuner: times every schedule on this batch's own boxes (one warm-up and
- * two timed steps each, CUDA events per sweep), keeps the fastest per axis and
+ * four timed steps each, CUDA events per sweep), keeps the fastest per axis and
  * restores the boxes' state and clocks.  Allocates a snapshot of the state
  * for the duration; waits for the device's queued work (steps of this handle
  * already enqueued on any stream finish first); synchronises.  Not under

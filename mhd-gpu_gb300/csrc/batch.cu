@@ -815,7 +815,7 @@ int mhdgpu_batch_tune(mhdgpu_batch *bt, mhdgpu_stream_t stream)
             }
             if (build_tables(*bt) != MHD_OK) continue;   // this schedule does not fit: skip it
             float tsum[3] = {0, 0, 0};
-            for (int rep = 0; rep < 3 && st == MHD_OK; ++rep) {
+            for (int rep = 0; rep < 5 && st == MHD_OK; ++rep) {
                 st = launch_step(*bt, s, ev, true);
                 if (st != MHD_OK) break;
                 if ((e = cudaEventSynchronize(ev[6])) != cudaSuccess) { st = bcuda(e, "mhdgpu_batch_tune"); break; }
