@@ -101,6 +101,30 @@ def test_workspace_sizes(L):
     assert L.mhdgpu_step_fused_workspace_bytes(32, 16, 8) == 8 * 32 * 16 * 8
 
 
+def test_path_choice_and_host_entries_without_a_gpu(L):
+    """MHD_PATH_AUTO's rule and its workspace, and the host-buffer entries'
+    argument checks, all answered on the host."""
+    import mhdgpu
+    fused, plain, auto = mhdgpu.MHD_PATH_FUSED, mhdgpu.MHD_PATH_PLAIN, mhdgpu.MHD_PATH_AUTO
+    assert L.mhdgpu_resolve_path(128, 128, 128) == fused
+    assert L.mhdgpu_resolve_path(512, 96, 64) == fused        # x pencils are always contiguous
+    assert L.mhdgpu_resolve_path(64, 256, 64) == plain
+    assert L.mhdgpu_resolve_path(64, 64, 129) == plain
+    for dims in ((128, 128, 128), (32, 256, 16)):
+        want = (L.mhdgpu_step_fused_workspace_bytes(*dims) if L.mhdgpu_resolve_path(*dims) == fused
+                else L.mhdgpu_step_workspace_bytes(*dims))
+        assert L.mhdgpu_path_workspace_bytes(*dims, auto) == want
+    assert L.mhdgpu_path_workspace_bytes(8, 8, 8, 9) == 0
+    P = C.c_void_p
+    fake, t = P(0x1000), C.c_float(0.0)
+    args = (0.7, 0, C.byref(t), 0.0, 1, None, None)
+    assert L.mhdgpu_run_host(None, fake, 8, 8, 8, *args, fused) == mhdgpu.MHD_ERR_ARG
+    assert L.mhdgpu_run_host(fake, fake, 8, 8, 8, *args, 9) == mhdgpu.MHD_ERR_ARG
+    assert L.mhdgpu_run_host(fake, fake, 0, 8, 8, *args, fused) == mhdgpu.MHD_ERR_ARG
+    assert L.mhdgpu_release_host_cache() == mhdgpu.MHD_OK   # nothing cached: a no-op
+    assert L.mhdgpu_batch_run_host(None, fake, fake, 1, None) == mhdgpu.MHD_ERR_ARG
+
+
 def test_batch_arguments_rejected_without_a_gpu(L):
     import mhdgpu
     P = C.c_void_p
