@@ -168,3 +168,23 @@ def test_oracle_matches_reference_run_on_shipped_32cube_state(oracle_lib):
     assert bits_equal(dts, g["dtsf"])
     assert hashlib.sha256(u.tobytes()).hexdigest() == str(g["uf_sha"][0])
     assert hashlib.sha256(b.tobytes()).hexdigest() == str(g["bf_sha"][0])
+
+
+def test_oracle64_keeps_div_b_and_conserves_on_a_noncubic_state(oracle_lib):
+    """Size-independent properties of the scheme, pinned on the FP64 oracle
+    with a turbulent non-cubic start: constrained transport keeps max |div B|
+    at round-off of the initial field, and mass and total energy (fluxes in
+    conservation form on a periodic box) are conserved to round-off."""
+    import ics
+    O = oracle_lib.oracle("f64")
+    nx, ny, nz = 24, 16, 20
+    u32, b32 = ics.random_state(nx, ny, nz, seed=12, amp=0.3)
+    u, b = u32.astype(np.float64), b32.astype(np.float64)
+    d0 = ics.div_b(b, nx, ny, nz)
+    t0 = ics.totals(u, nx, ny, nz)
+    s, _t, _dts = O.run(u, b, nx, ny, nz, cfl_number=0.7, tf=0.0, max_steps=6)
+    assert s == 6
+    assert ics.div_b(b, nx, ny, nz) < d0 + 1e-12
+    t1 = ics.totals(u, nx, ny, nz)
+    assert abs(t1[0] - t0[0]) < 1e-12 * abs(t0[0])
+    assert abs(t1[4] - t0[4]) < 1e-12 * abs(t0[4])
