@@ -54,9 +54,13 @@ sys.path.insert(0, os.path.join(REPO, "oracle"))
 METRIC = "cell-updates/s per full MHD step, fused+batched vs plain; % of HBM roofline"
 UNIT = "cell-updates/s"
 FLUIDX_BYTES_PER_CELL = 52      # R u 20 + b 12, W u 20 (one read and write of the pencil data)
-# one sweep of the batched kernel per cell: fluid 52 (above); field 32 (R rho, m 8,
-# R b2 b3 8, W b2 b3 8, W sA sB 8); b(1) 16 (R sA sB 8, R+W b1 8)
-SWEEP_BYTES_PER_CELL = 100
+# Algorithmic bytes of one sweep per cell: one read and one write of the 8-float
+# state (32 R + 32 W), the basis the roofline fraction is quoted on.
+SWEEP_BYTES_PER_CELL = 64
+# The bytes the current sweep actually has to move per cell, as a diagnostic:
+# fluid 52 (above); field 32 (R rho, m 8, R b2 b3 8, W b2 b3 8, W sA sB 8);
+# b(1) 16 (R sA sB 8, R+W b1 8)
+SWEEP_PASS_BYTES_PER_CELL = 100
 STEP_BYTES_64 = 64              # one read + one write of the 8-float state per cell-update
 # floating-point operations per cell-update of one full step (6 fluid and 6 field
 # sweeps + the CFL reduction), counted on the oracle as the reference writes
@@ -256,6 +260,119 @@ def cpu_rate_ensemble(ens, seconds, threads):
                                        f"({cells / 1e6:.1f} M cell-updates, {el:.1f} s)")
 
 
+def host_cpu():
+    """The host CPU's model name (lscpu), for the CPU-baseline record."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    return "unknown"
+
+
+def reference_arm(args, config, ens_mode, n, K, W):
+    """--impl reference: the reference algorithm's CPU implementation on this
+    host's cores, on the same workload, metric and config as the GPU arm.
+    The reference's own C path compiled from its sources (oracle/_ref) is timed
+    where it was built and the workload is a cubic box; otherwise the oracle
+    port (bit-identical to that C path, OpenMP over pencils).  Each timed step
+    is one whole step of the workload (all 64 boxes of the ensemble); the
+    number of timed steps is K capped so that the timed work stays near a
+    minute, and the line reports the steps that ran.  A 1-core rate of the same
+    code is reported beside it."""
+    if int(os.environ.get("RANK", "0")) != 0:
+        return
+    import numpy as np
+    import oracle as O
+    import ics
+    threads = os.cpu_count() or 1
+    if not os.path.exists(O.LIB_ORACLE):
+        subprocess.run(["make", "-s", "-C", os.path.join(REPO, "oracle")], check=True)
+    cap_s = 60.0
+    if ens_mode:
+        ens = ics.ensemble(**ENSEMBLE)
+        cells = sum(e["dims"][0] * e["dims"][1] * e["dims"][2] for e in ens)
+        P, kind, cores = _cpu_path(threads, False)
+        states = [(e["u"].copy(), e["b"].copy(), e["dims"]) for e in ens]
+
+        def one_step():
+            for u, b, d in states:
+                P.step(u, b, *d, P.dt_from_cfl(P.calcfl(u, b, *d), CFL, np.float32(0), np.float32(0)))
+
+        for w in range(W):   # warm-up: W box-steps (the first pages everything in)
+            u, b, d = states[w % len(states)]
+            P.step(u, b, *d, P.dt_from_cfl(P.calcfl(u, b, *d), CFL, np.float32(0), np.float32(0)))
+        what = "the 64 boxes of the ensemble"
+    else:
+        cells = n ** 3
+        use_ref = O.ref_available("f32")
+        P, kind, cores = _cpu_path(threads, use_ref)
+        u, b = ics.alfven_oblique(n)
+
+        def one_step():
+            P.step(u, b, n, n, n, P.dt_from_cfl(P.calcfl(u, b, n, n, n), CFL, np.float32(0), np.float32(0)))
+
+        for _ in range(W):
+            one_step()
+        what = f"the {n}^3 box"
+    times = []
+    t_all = time.perf_counter()
+    while len(times) < K:
+        t0 = time.perf_counter()
+        one_step()
+        times.append(time.perf_counter() - t0)
+        if time.perf_counter() - t_all + times[-1] > cap_s:
+            break
+    secs = sum(times)
+    rate = cells * len(times) / secs
+    sample = (f"{len(times)} timed steps of {what} ({cells * len(times) / 1e6:.1f} M cell-updates, "
+              f"{secs:.1f} s) after {W} warm-up {'box-steps' if ens_mode else 'steps'}; "
+              f"{cores} threads on {host_cpu()}")
+    one = None
+    if ens_mode:
+        r1, k1, c1, s1 = cpu_rate_ensemble(ens, 8.0, 1)
+        one = {"value": r1, "unit": UNIT, "cores": c1, "kind": k1, "sample": s1}
+    else:
+        r1, k1, c1, s1 = cpu_rate(n, 8.0, 1, O.ref_available("f32"))
+        one = {"value": r1, "unit": UNIT, "cores": c1, "kind": k1, "sample": s1}
+    print(json.dumps({
+        "metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": args.gpus, "steps": len(times),
+        "steps_requested": K, "warmup": W, "ms_per_step": secs / len(times) * 1e3,
+        "higher_is_better": True, "scaling": "strong" if ens_mode else "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic", "config": config, "impl": "reference",
+        "cpu_baseline": {"value": rate, "unit": UNIT, "cores": cores, "kind": kind, "sample": sample},
+        "cpu_baseline_1core": one,
+        "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }))
+
+
+def spawn_ranks(n_gpus):
+    """--gpus N without a launcher: re-run this command under torch.distributed.run
+    with N ranks on this node (one per GPU), after checking that N GPUs are
+    visible.  Under a launcher, WORLD_SIZE must equal N."""
+    env_world = os.environ.get("WORLD_SIZE")
+    if env_world is not None:
+        if int(env_world) != n_gpus:
+            sys.exit(f"bench.py: --gpus {n_gpus} but WORLD_SIZE={env_world}")
+        return
+    if n_gpus <= 1:
+        return
+    import torch
+    have = torch.cuda.device_count()
+    if have < n_gpus:
+        sys.exit(f"bench.py: --gpus {n_gpus} asked for, {have} visible")
+    import socket
+    with socket.socket() as sk:
+        sk.bind(("127.0.0.1", 0))
+        port = sk.getsockname()[1]
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", f"--nproc-per-node={n_gpus}",
+           "--master-addr", "127.0.0.1", "--master-port", str(port), os.path.abspath(__file__),
+           *sys.argv[1:]]
+    os.execv(sys.executable, cmd)
+
+
 # ---------------------------------------------------------------- GPU timing
 def timed_replays(graph_fn, K, W, stream, flush, world):
     """K graph replays bracketed by CUDA events on `stream`, L2 flushed before
@@ -417,6 +534,7 @@ def ensemble_bench(ens, K, W, stream, flush, world, dev, tune, total_cells):
     avg_s = b_ms / 1e3 / max(b_rec, 1)
     hbm, kind = peaks()
     ach = SWEEP_BYTES_PER_CELL * cells / avg_s / 1e9
+    pass_ach = SWEEP_PASS_BYTES_PER_CELL * cells / avg_s / 1e9
     tot_ms = sum(v[2] for v in summ.values())
     res = {"value": value, "ms_per_step": secs / K * 1e3, "cells": cells, "schedule": sched,
            "schedule_from": "mhdgpu_batch_tune" if tune else "defaults", "wall": wall,
@@ -430,6 +548,11 @@ def ensemble_bench(ens, K, W, stream, flush, world, dev, tune, total_cells):
                         "peak_source": f"{kind} (MEASURED_PEAKS.json hbm_gbs)",
                         "traffic": read_traffic("batch_class_ensemble64_ncu.txt"),
                         "algorithmic_bytes_per_launch": SWEEP_BYTES_PER_CELL * cells,
+                        "algorithmic_basis": "64 B/cell per sweep: one read and one write of the "
+                                             "8-float state",
+                        "pass_bytes_diagnostic": {"bytes_per_cell": SWEEP_PASS_BYTES_PER_CELL,
+                                                  "what": "fluid 52 + field flux 32 + b(1) gather 16",
+                                                  "achieved_gbs": pass_ach, "frac": pass_ach / hbm},
                         "launch_unit": "one sweep (its class launches together)",
                         "avg_launch_us": avg_s * 1e6,
                         "share_of_step": b_ms / tot_ms if tot_ms else None}}
@@ -534,6 +657,9 @@ def main():
     args = ap.parse_args()
     n, K, W = args.n, args.steps, max(3, args.warmup)
     ens_mode = args.workload == "ensemble64"
+    if args.impl == "ours":
+        spawn_ranks(args.gpus)
+    world_hint = int(os.environ.get("WORLD_SIZE", args.gpus))
     if ens_mode:
         config = {"workload": "ensemble64", "boxes": ENSEMBLE["nbox"], "sizes": list(ENSEMBLE["sizes"]),
                   "seed": ENSEMBLE["seed"], "amp_range": list(ENSEMBLE["amp_range"]),
@@ -543,39 +669,25 @@ def main():
                   "path": "batched: per sweep one persistent launch per pencil-length class over all "
                           "boxes, the classes concurrent, one CUDA graph per step",
                   "l2": "flushed between timed steps (512 MB write, outside the timed events); state 0.87 GB > L2",
-                  "parallelism": f"boxes sharded across {args.gpus} rank(s), balanced by cells"}
+                  "parallelism": f"boxes sharded across {world_hint} rank(s), balanced by cells"}
+        import ics
+        import shard
+        ens_dims = ics.ensemble_dims(**ENSEMBLE)
+        parts = shard.partition_boxes(ens_dims, world_hint)
+        config["shard"] = {"ranks": world_hint, "boxes_per_rank": [len(p) for p in parts],
+                           "cells_per_rank": shard.shard_cells(ens_dims, parts)}
     else:
         config = {"workload": f"alfven_diag_{n}", "box": [n, n, n], "cfl": CFL, "cfl_mode": "c_path",
                   "ic": "linear Alfven wave, k=(1,1,1)2pi/L, A=1e-3, rho=p=1, B0 along k",
                   "path": "transpose-free step (mhdgpu_step_fused), one CUDA graph per step",
                   "l2": "flushed between timed steps (512 MB write, outside the timed events)",
-                  "parallelism": f"replicas x{args.gpus}"}
+                  "parallelism": f"replicas x{world_hint}"}
+    # the arithmetic: the faithful policy reproduces the reference C path's
+    # rounding (the CPU arm runs that path's restatement); "fast" is plain FP32
+    config["math"] = args.math
 
     if args.impl == "reference":
-        rank = int(os.environ.get("RANK", "0"))
-        if rank != 0:
-            return
-        threads = os.cpu_count() or 1
-        if not os.path.exists(os.path.join(REPO, "oracle", "lib", "liboracle.so")):
-            subprocess.run(["make", "-s", "-C", os.path.join(REPO, "oracle")], check=True)
-        budget = min(120.0, max(10.0, 0.25 * (K + W)))
-        if ens_mode:
-            import ics
-            ens = ics.ensemble(**ENSEMBLE)
-            rate, kind, cores, sample = cpu_rate_ensemble(ens, budget, threads)
-            ms = sum(e["dims"][0] * e["dims"][1] * e["dims"][2] for e in ens) / rate * 1e3
-        else:
-            use_ref = os.path.exists(os.path.join(REPO, "oracle", "_ref", "libref_f32.so"))
-            rate, kind, cores, sample = cpu_rate(n, budget, threads, use_ref)
-            ms = n ** 3 / rate * 1e3
-        print(json.dumps({
-            "metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": args.gpus, "steps": K,
-            "warmup": W, "ms_per_step": ms, "higher_is_better": True,
-            "scaling": "strong" if ens_mode else "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic", "config": config, "impl": "reference",
-            "cpu_baseline": {"value": rate, "unit": UNIT, "cores": cores, "kind": kind, "sample": sample},
-            "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        }))
+        reference_arm(args, config, ens_mode, n, K, W)
         return
 
     import torch
@@ -587,7 +699,6 @@ def main():
     dev = torch.device("cuda", local if world > 1 else 0)
     math_mode = mhdgpu.MHD_MATH_FAST if args.math == "fast" else mhdgpu.MHD_MATH_FAITHFUL
     mhdgpu.set_math(math_mode)
-    config["math"] = args.math
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
     stream = torch.cuda.Stream(device=dev)
     vis = [x.strip() for x in os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",") if x.strip()]
@@ -641,8 +752,6 @@ def main():
         # (balanced by cells), no exchange on the data path
         parts = shard.partition_boxes([e["dims"] for e in ens], world)
         mine = [ens[i] for i in parts[rank]]
-        config["shard"] = {"ranks": world, "boxes_per_rank": [len(p) for p in parts],
-                           "cells_per_rank": shard.shard_cells([e["dims"] for e in ens], parts)}
         eb = ensemble_bench(mine, K, W, stream, flush, world, dev, tune, total_cells)
         sampler.stop()
         clocks = sampler.summary(*eb["wall"])
@@ -656,7 +765,7 @@ def main():
             "gpu_launches": int(round(sum(launches.values()) * K)),
             "roofline": out_roof,
             "roofline_step": roofline_step(value, world, out_roof["peak"], dev, clocks,
-                                           SWEEP_BYTES_PER_CELL * 6),
+                                           SWEEP_PASS_BYTES_PER_CELL * 6),
             "plain_drop_in": {"value": eb["boxwise_plain"]["value"], "unit": UNIT,
                               "ms_per_step": eb["boxwise_plain"]["ms_per_step"],
                               "path": eb["boxwise_plain"]["path"]},
@@ -677,7 +786,7 @@ def main():
             "gpu_launches": int(round(sum(fused["kernel_launches_per_step"].values()) * K)),
             "roofline": sb["fluidx_roofline"],
             "roofline_step": roofline_step(fused["value"], world, sb["fluidx_roofline"]["peak"], dev, clocks,
-                                           SWEEP_BYTES_PER_CELL * 6),
+                                           SWEEP_PASS_BYTES_PER_CELL * 6),
             "plain_drop_in": {"value": sb["plain"]["value"], "unit": UNIT,
                               "ms_per_step": sb["plain"]["ms_per_step"], "path": sb["plain"]["path"]},
             "fused_over_plain": sb["fused_over_plain"],
@@ -693,7 +802,12 @@ def main():
                 use_ref = os.path.exists(os.path.join(REPO, "oracle", "_ref", "libref_f32.so"))
                 rate, kind, cores, sample = cpu_rate(n, args.cpu_seconds, os.cpu_count() or 1, use_ref)
             out["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": cores, "kind": kind,
-                                   "sample": sample}
+                                   "sample": sample + f"; {host_cpu()}"}
+            if ens_mode:
+                r1, k1, c1, s1 = cpu_rate_ensemble(ens, 6.0, 1)
+            else:
+                r1, k1, c1, s1 = cpu_rate(n, 6.0, 1, use_ref)
+            out["cpu_baseline_1core"] = {"value": r1, "unit": UNIT, "cores": c1, "kind": k1, "sample": s1}
         except Exception as e:  # noqa: BLE001
             out["cpu_baseline"] = {"value": None, "unit": UNIT, "error": str(e)}
     if rank == 0:

@@ -99,7 +99,9 @@ int mhdgpu_advectbyzx(float *b, const float *u, int nx, int ny, int nz,
  * it.  It allocates nothing.  Boxes above MHD_NOALLOC_MAX_CELLS cells are
  * rejected with MHD_ERR_ARG.  The first call on a device looks up the array's
  * device address with that device current; make it before any stream
- * capture.  All calls share the array, so calls that overlap on the GPU race
+ * capture.  mhdgpu_release_host_cache forgets those addresses: call it before
+ * a device reset, and the next call on the device looks the address up again
+ * (so that call, too, must come before any capture).  All calls share the array, so calls that overlap on the GPU race
  * and must be serialised by the caller.  Nothing in the array has to start at
  * zero: each call writes every entry it reads. */
 #define MHD_NOALLOC_MAX_CELLS 2097152   /* 128^3 */
@@ -220,7 +222,8 @@ int mhdgpu_advance(float *u, float *b, int nx, int ny, int nz, int nsteps,
 int mhdgpu_run_host(float *u, float *b, int nx, int ny, int nz, double cfl_number,
                     int cfl_mode, float *t, float tf, int max_steps, float *dt_log,
                     int *steps_done, int path);
-/* Frees the calling thread's device buffers and stream of mhdgpu_run_host
+/* Frees the calling thread's device buffers and stream of mhdgpu_run_host,
+ * and drops the device addresses that mhdgpu_advectbyzx_noalloc looked up
  * (call it before resetting the device from that thread). */
 int mhdgpu_release_host_cache(void);
 

@@ -333,6 +333,13 @@ int mhdgpu_advance(float *u, float *b, int nx, int ny, int nz, int nsteps, doubl
     if (path == MHD_PATH_AUTO) path = mhdgpu_resolve_path(nx, ny, nz);
     if (path != MHD_PATH_PLAIN && path != MHD_PATH_FUSED)
         return fail(MHD_ERR_ARG, "mhdgpu_advance: bad path");
+    // Every check of the step runs here, before the first launch: a call that
+    // is rejected queues nothing and leaves the clock as it was.
+    int st0 = check_dims(nx, ny, nz, "mhdgpu_advance");
+    if (st0) return st0;
+    if (ny > MHD_MAX_PENCIL || nz > MHD_MAX_PENCIL)
+        return fail(MHD_ERR_ARG, "mhdgpu_advance: every axis becomes a pencil; each must be <= MHD_MAX_PENCIL");
+    if (!u || !b || !d_work) return fail(MHD_ERR_ARG, "mhdgpu_advance: null state or workspace pointer");
     cudaStream_t s = (cudaStream_t)stream;
     // The CFL reduction runs as its own pass before the first step of the
     // call (unless the caller resumes); every step's last fluid sweep folds
@@ -462,6 +469,7 @@ done:
 int mhdgpu_release_host_cache(void)
 {
     g_host_cache.release();
+    noalloc_forget_devices();
     return MHD_OK;
 }
 

@@ -92,6 +92,8 @@ cudaError_t launch_clock(mhdgpu_clock *clk, double cfl_number, float tf, float *
 
 // sets the calling thread's message returned by mhdgpu_last_error()
 void set_last_error(const char *msg);
+// drops mhdgpu_advectbyzx_noalloc's per-device scratch addresses (noalloc.cu)
+void noalloc_forget_devices();
 
 // Raises a kernel's dynamic shared-memory limit to smem when above the 48 KB
 // default, once per device and size (cache: one word per device ordinal;

@@ -14,7 +14,10 @@
 // process exits.  Its name is only a host-side stand-in in host code, so the
 // device address is looked up once per device with cudaGetSymbolAddress, with
 // that device current, on the first call made while it is the current device;
-// make that first call before any stream capture.  Every call shares the one
+// make that first call before any stream capture.  mhdgpu_release_host_cache
+// forgets the looked-up addresses (a device reset unloads the module and the
+// array may come back elsewhere), so the next call looks them up again.
+// Every call shares the one
 // array: calls that overlap on the GPU (different streams, or threads using
 // the same device) race on it and must be serialised by the caller.  The
 // flux kernel writes every scratch entry it covers before the gather kernel
@@ -26,6 +29,7 @@
 #include <mutex>
 
 #include "kernels.cuh"
+#include "profiler.cuh"
 
 namespace {
 
@@ -71,6 +75,14 @@ int scratch_on_current_device(float **out)
 
 }  // namespace
 
+// Called by mhdgpu_release_host_cache: after a device reset the array's old
+// address is no longer valid, so every device looks it up again.
+void mhd::noalloc_forget_devices()
+{
+    std::lock_guard<std::mutex> lock(g_setup_mutex);
+    for (int d = 0; d < kMaxDevices; ++d) g_scratch_ptr[d] = nullptr;
+}
+
 extern "C" {
 
 int mhdgpu_advectbyzx_noalloc(float *b, const float *u, int nx, int ny, int nz, const float *d_dt,
@@ -88,6 +100,7 @@ int mhdgpu_advectbyzx_noalloc(float *b, const float *u, int nx, int ny, int nz, 
     int st = scratch_on_current_device(&scr);
     if (st != MHD_OK) return st;
     mhd::AdvectArgs a = mhd::make_advect_args(b, u, d_dt, scr, scr + ncell, mhd::make_frame(nx, ny, nz));
+    mhd::ProfScope ps(MHD_KCLASS_ADVECT, 2, (cudaStream_t)stream);
     cudaError_t e = mhd::launch_advect(a, mhd::pencil_cfg(MHD_KCLASS_ADVECT, nx), mhd::math_mode(), (cudaStream_t)stream);
     if (e != cudaSuccess) return noalloc_cuda_fail("launch", e);
     return MHD_OK;

@@ -149,6 +149,25 @@ def turbulence(nx, ny=None, nz=None, seed=0, mach=0.5, b_mean=0.3, db_rms=None, 
     return _pack(rho, m, e, db, dtype)
 
 
+def ensemble_specs(nbox=64, seed=0, sizes=(32, 48, 64, 96, 128), amp_range=(1e-4, 1e-1)):
+    """The draws of ensemble() without building the states: a list of dicts
+    {dims: (nx, ny, nz), kind, amp, seed}, in box order."""
+    r = np.random.default_rng(seed)
+    out = []
+    for _ in range(nbox):
+        dims = tuple(int(x) for x in r.choice(sizes, size=3))
+        amp = float(np.exp(r.uniform(np.log(amp_range[0]), np.log(amp_range[1]))))
+        kind = "alfven" if r.random() < 0.5 else "turbulent"
+        bseed = int(r.integers(0, 2 ** 31 - 1))
+        out.append({"dims": dims, "kind": kind, "amp": amp, "seed": bseed})
+    return out
+
+
+def ensemble_dims(nbox=64, seed=0, sizes=(32, 48, 64, 96, 128), amp_range=(1e-4, 1e-1)):
+    """The box sizes of ensemble(), cheaply."""
+    return [e["dims"] for e in ensemble_specs(nbox, seed, sizes, amp_range)]
+
+
 def ensemble(nbox=64, seed=0, sizes=(32, 48, 64, 96, 128), amp_range=(1e-4, 1e-1),
              dtype=np.float32):
     """The batched-ensemble workload: nbox independent periodic boxes whose
@@ -158,18 +177,14 @@ def ensemble(nbox=64, seed=0, sizes=(32, 48, 64, 96, 128), amp_range=(1e-4, 1e-1
     amplitude drawn log-uniformly from amp_range.
 
     Returns a list of dicts {dims: (nx, ny, nz), kind, amp, seed, u, b}."""
-    r = np.random.default_rng(seed)
     out = []
-    for i in range(nbox):
-        dims = tuple(int(x) for x in r.choice(sizes, size=3))
-        amp = float(np.exp(r.uniform(np.log(amp_range[0]), np.log(amp_range[1]))))
-        kind = "alfven" if r.random() < 0.5 else "turbulent"
-        bseed = int(r.integers(0, 2 ** 31 - 1))
-        if kind == "alfven":
+    for e in ensemble_specs(nbox, seed, sizes, amp_range):
+        dims, amp = e["dims"], e["amp"]
+        if e["kind"] == "alfven":
             u, b = alfven_oblique(dims[0], amp=amp, ny=dims[1], nz=dims[2], dtype=dtype)
         else:
-            u, b = turbulence(*dims, seed=bseed, v_rms=amp, db_rms=amp, dtype=dtype)
-        out.append({"dims": dims, "kind": kind, "amp": amp, "seed": bseed, "u": u, "b": b})
+            u, b = turbulence(*dims, seed=e["seed"], v_rms=amp, db_rms=amp, dtype=dtype)
+        out.append(dict(e, u=u, b=b))
     return out
 
 

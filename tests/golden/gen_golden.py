@@ -86,10 +86,13 @@ def write_alfven32(ref, R):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default=os.environ.get("MHD_REFERENCE", "/root/reference"))
+    ap.add_argument("--ref", default=os.environ.get("MHD_REFERENCE"),
+                    help="pandaPQY/MHD-GPU checkout (or set MHD_REFERENCE)")
     ap.add_argument("--only-digest", action="store_true")
     ap.add_argument("--only-alfven32", action="store_true")
     args = ap.parse_args()
+    if not args.ref:
+        ap.error("give --ref <pandaPQY/MHD-GPU checkout> or set MHD_REFERENCE")
     write_digest(args.ref)
     if args.only_digest:
         return

@@ -67,6 +67,16 @@ def test_bad_arguments_are_rejected_without_a_gpu(L):
     assert L.mhdgpu_advance(fake, fake, 8, 8, 8, -1, 0.9, 0, 0.0, fake, None, fake, 0, None) == mhdgpu.MHD_ERR_ARG
     assert L.mhdgpu_advance(fake, fake, 8, 8, 8, 1, 0.0, 0, 0.0, fake, None, fake, 0, None) == mhdgpu.MHD_ERR_ARG
     assert L.mhdgpu_advance(fake, fake, 8, 8, 8, 1, 0.9, 0, 0.0, fake, None, fake, 5, None) == mhdgpu.MHD_ERR_ARG
+    # the step's own checks run before the CFL pass and the clock tick: with a
+    # valid-looking clock, a null state, a null workspace or a y/z axis above
+    # the pencil limit are rejected without a launch (no GPU is touched here)
+    assert L.mhdgpu_advance(None, fake, 8, 8, 8, 1, 0.9, 0, 0.0, fake, None, fake, 0, None) == mhdgpu.MHD_ERR_ARG
+    assert L.mhdgpu_advance(fake, None, 8, 8, 8, 1, 0.9, 0, 0.0, fake, None, fake, 1, None) == mhdgpu.MHD_ERR_ARG
+    assert L.mhdgpu_advance(fake, fake, 8, 8, 8, 1, 0.9, 0, 0.0, fake, None, None, 0, None) == mhdgpu.MHD_ERR_ARG
+    assert b"null" in L.mhdgpu_last_error()
+    assert L.mhdgpu_advance(fake, fake, 8, 2000, 8, 1, 0.9, 0, 0.0, fake, None, fake, 1, None) == mhdgpu.MHD_ERR_ARG
+    assert b"MHD_MAX_PENCIL" in L.mhdgpu_last_error()
+    assert L.mhdgpu_advance(fake, fake, 0, 8, 8, 1, 0.9, 0, 0.0, fake, None, fake, 0, None) == mhdgpu.MHD_ERR_ARG
     assert L.mhdgpu_step_fused(fake, fake, 8, 2000, 8, fake, fake, None, None) == mhdgpu.MHD_ERR_ARG
     assert L.mhdgpu_dt_update(fake, -1.0, 0.0, fake, fake, None) == mhdgpu.MHD_ERR_ARG
 
