@@ -221,15 +221,17 @@ __device__ __forceinline__ void fluidx_tile_team(const FluidxArgs &a, long long 
             cl = fmaxf(cl, cs);
         }
         const float c = tm.pencil_max(cl, rq);
-        const bool cpos = c > 0.0f;
-        const float yc = cpos ? M::recip(c) : 0.0f;
+        // v/c where c > 0 (mhdflux.c:48-57); where c = 0 the quotient by 1
+        // leaves every finite v as it is, without a select per value
+        const float cd = c > 0.0f ? c : 1.0f;
+        const float yc = M::recip(cd);
         // fr = c(u + v/c) kept in u1[]; wl exchanged
 #pragma unroll
         for (int m = 0; m < CPL; ++m)
 #pragma unroll
             for (int ii = 0; ii < 5; ++ii) if (tm.valid(m)) {
                 const float uu = us[tm.ci(m) * 5 + ii];
-                const float vv = cpos ? M::divy(v[m][ii], c, yc) : v[m][ii];
+                const float vv = M::divy(v[m][ii], cd, yc);
                 u1[m][ii] = M::mul(c, M::add(uu, vv));
                 tm.put(X(ii), m, M::sub(uu, vv));
             }
@@ -271,13 +273,15 @@ __device__ __forceinline__ void fluidx_tile_team(const FluidxArgs &a, long long 
             }
             const float c = tm.pencil_max(cl, rq);
             cl = c;
-            const bool cpos = c > 0.0f;
-            const float yc = cpos ? M::recip(c) : 0.0f;
+            // v/c where c > 0 (mhdflux.c:48-57); where c = 0 the quotient by 1
+            // leaves every finite v as it is, without a select per value
+            const float cd = c > 0.0f ? c : 1.0f;
+            const float yc = M::recip(cd);
 #pragma unroll
             for (int m = 0; m < CPL; ++m)
 #pragma unroll
                 for (int ii = 0; ii < 5; ++ii) if (tm.valid(m)) {
-                    const float vv = cpos ? M::divy(v[m][ii], c, yc) : v[m][ii];
+                    const float vv = M::divy(v[m][ii], cd, yc);
                     tm.put(X(ii), m, M::mul(c, M::add(u1[m][ii], vv)));
                     tm.put(X(5 + ii), m, M::sub(u1[m][ii], vv));
                 }

@@ -316,8 +316,10 @@ __device__ __forceinline__ void fluidx_tile_reg(const FluidxArgs &a, long long t
             }
         }
         const float c = ln.max(cl);
-        const bool cpos = c > 0.0f;
-        const float yc = cpos ? M::recip(c) : 0.0f;
+        // v/c where c > 0 (mhdflux.c:48-57); where c = 0 the quotient by 1
+        // leaves every finite v as it is, without a select per value
+        const float cd = c > 0.0f ? c : 1.0f;
+        const float yc = M::recip(cd);
 #pragma unroll
         for (int ii = 0; ii < 5; ++ii) {
             float uu[CPL], wl[CPL], fl[CPL];
@@ -325,7 +327,7 @@ __device__ __forceinline__ void fluidx_tile_reg(const FluidxArgs &a, long long t
             // fr = c(u + v/c) (kept in u1), wl = u - v/c
 #pragma unroll
             for (int m = 0; m < CPL; ++m) {
-                const float vv = cpos ? M::divy(v[m][ii], c, yc) : v[m][ii];
+                const float vv = M::divy(v[m][ii], cd, yc);
                 u1[m][ii] = M::mul(c, M::add(uu[m], vv));
                 wl[m] = M::sub(uu[m], vv);
             }
@@ -354,8 +356,10 @@ __device__ __forceinline__ void fluidx_tile_reg(const FluidxArgs &a, long long t
             if (!(p > 0.0f)) bad |= MHD_HEALTH_PRESSURE;
         }
         const float c = ln.max(cl);
-        const bool cpos = c > 0.0f;
-        const float yc = cpos ? M::recip(c) : 0.0f;
+        // v/c where c > 0 (mhdflux.c:48-57); where c = 0 the quotient by 1
+        // leaves every finite v as it is, without a select per value
+        const float cd = c > 0.0f ? c : 1.0f;
+        const float yc = M::recip(cd);
         const float mdt = -dt;
         float ssum[CPL];
 #pragma unroll
@@ -366,7 +370,7 @@ __device__ __forceinline__ void fluidx_tile_reg(const FluidxArgs &a, long long t
             float fr[CPL], fl[CPL];
 #pragma unroll
             for (int m = 0; m < CPL; ++m) {
-                const float vv = cpos ? M::divy(v[m][ii], c, yc) : v[m][ii];
+                const float vv = M::divy(v[m][ii], cd, yc);
                 fr[m] = M::mul(c, M::add(u1[m][ii], vv));
                 fl[m] = M::mul(c, M::sub(u1[m][ii], vv));
             }
