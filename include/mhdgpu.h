@@ -228,7 +228,10 @@ int mhdgpu_run_host(float *u, float *b, int nx, int ny, int nz, double cfl_numbe
 int mhdgpu_release_host_cache(void);
 
 /* ------------------------------------------------------------------------
- * Arithmetic policy and tile shapes (process-wide settings, host side).
+ * Arithmetic policy and row staging (settings of the calling host thread:
+ * a setting made on one thread changes only the launches that thread makes,
+ * and a CUDA graph keeps the settings it was captured with), and tile shapes
+ * (a process-wide table; a shape changes the speed, never the result).
  * ------------------------------------------------------------------------ */
 #define MHD_MATH_FAITHFUL   0   /* rounding of the reference C path (default) */
 #define MHD_MATH_FAST       1   /* plain FP32 with FMA contraction, hardware
@@ -244,6 +247,18 @@ int mhdgpu_release_host_cache(void);
 
 /* selects the policy of the fluid kernels; returns the previous one */
 int mhdgpu_set_math(int mode);
+
+/* How the transpose-free step moves the pencils that run across memory (its
+ * y and z sweeps) between global and shared memory:
+ *   MHD_STAGING_TMA (default): where the frame allows (pencils of 32, 64 or
+ *     128 cells in teams of one warp, 8 per CTA, every row stride a multiple
+ *     of 4 cells, 16-byte aligned arrays) the fluid tile is loaded and stored
+ *     by tensor copies of the Tensor Memory Accelerator;
+ *   MHD_STAGING_CPASYNC: every row is moved by 4-byte asynchronous copies.
+ * Both give the same bits.  Returns the previous mode (-1 for a bad mode). */
+#define MHD_STAGING_TMA      0
+#define MHD_STAGING_CPASYNC  1
+int mhdgpu_set_row_staging(int mode);
 
 /* Team shape of a pencil kernel (kclass MHD_KCLASS_FLUIDX or
  * MHD_KCLASS_ADVECT, OR-ed with MHD_TILE_ROWS for pencils that run across

@@ -399,11 +399,36 @@ fluidx_kernel(FluidxArgs a)
     fluidx_tile<CPL, WPP, M, ROWS, NT, true>(a, blockIdx.x);
 }
 
+// The row-staged sweep with its tile moved by TMA (tma_rows.cuh): pencils
+// that fill one warp (NT = 32 CPL), kTmaPencils per CTA, in place.
+template <int CPL, class M, int NT>
+__global__ void __launch_bounds__(32 * kTmaPencils)
+fluidx_kernel_tma(const __grid_constant__ FluidxArgs a, const __grid_constant__ RowMaps maps)
+{
+    fluidx_tile_reg<CPL, 32, M, true, true, true>(a, blockIdx.x, &maps);
+}
+
 // Launch one instantiation; sets the dynamic shared-memory attribute once per
 // instantiation when above the 48 KB default.
 template <int CPL, int WPP, class M, bool ROWS, int NT>
 cudaError_t launch_fluidx_inst(const FluidxArgs &a, int ppc, cudaStream_t s)
 {
+    if constexpr (ROWS && WPP == 1 && NT == 32 * CPL) {
+        // row-staged pencils that fill a warp: through TMA when the frame allows
+        RowMaps maps;
+        if (row_staging() == MHD_STAGING_TMA && ppc == kTmaPencils && a.u_out == a.u_in &&
+            tma_rows_encode(&maps, a.u_in, a.b, a.f.n, a.f.ny, a.f.nz, a.f.si, a.f.sk, kTmaPencils)) {
+            static std::atomic<size_t> smem_tma[kSmemCacheDevices];
+            const size_t smem = sizeof(float) * (size_t)txr_smem_floats(fxr_smem_floats(NT, ppc, true), NT);
+            if (smem > 227 * 1024) return cudaErrorInvalidConfiguration;
+            const cudaError_t e =
+                ensure_dynamic_smem((const void *)fluidx_kernel_tma<CPL, M, NT>, smem, smem_tma);
+            if (e != cudaSuccess) return e;
+            const long long blocks = (long long)((a.f.ny + ppc - 1) / ppc) * a.f.nz;
+            fluidx_kernel_tma<CPL, M, NT><<<(unsigned)blocks, 32 * ppc, smem, s>>>(a, maps);
+            return cudaGetLastError();
+        }
+    }
     static std::atomic<size_t> smem_set[kSmemCacheDevices];
     const int threads = 32 * WPP * ppc;
     const long long blocks = ROWS ? (long long)((a.f.ny + ppc - 1) / ppc) * a.f.nz

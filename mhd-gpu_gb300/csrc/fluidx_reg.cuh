@@ -20,6 +20,7 @@
 #pragma once
 
 #include "kernels.cuh"
+#include "tma_rows.cuh"
 
 namespace mhd {
 
@@ -110,8 +111,10 @@ __device__ __forceinline__ void load_comp(const float *p, bool live, int ii, flo
 // GROUPED: rows mode moves its rows in groups of four with per-lane offsets
 // fixed for the tile (fewer copy instructions, more registers held); the
 // single-box kernels take it, the register-capped batch kernels do not.
-template <int CPL, int TPP, class M, bool ROWS, bool GROUPED = false>
-__device__ __forceinline__ void fluidx_tile_reg(const FluidxArgs &a, long long tile)
+// TMA: rows mode stages the tile and writes it back through tensor copies
+// (tma_rows.cuh; tm holds the frame's maps, ppc = kTmaPencils, in place).
+template <int CPL, int TPP, class M, bool ROWS, bool GROUPED = false, bool TMA = false>
+__device__ __forceinline__ void fluidx_tile_reg(const FluidxArgs &a, long long tile, const RowMaps *tm = nullptr)
 {
     constexpr int N = TPP * CPL;
     constexpr int CS = N + 4, PS = 5 * CS, BSC = 3 * N, BSR = 3 * N + 4, KS = N + 4;
@@ -181,7 +184,12 @@ __device__ __forceinline__ void fluidx_tile_reg(const FluidxArgs &a, long long t
             const long long kpb = (long long)kp * f.sk;
             float *SB = BS;                          // (ppc+1) * BSR: b of columns j0 .. j0+nvalid
             float *SK = BS + (ppc + 1) * BSR;        // ppc * KS: b(3) of plane k+1, [pencil][i]
-            if constexpr (GROUPED) {
+            if constexpr (TMA) {
+                float *raw = txr_raw(smem, fxr_smem_floats(N, ppc, true));
+                uint64_t *bar = reinterpret_cast<uint64_t *>(raw + txr_raw_floats(N));
+                if (!tma_rows_stage<N>(f, *tm, US, PS, CS, SB, BSR, SK, KS, raw, bar, j0, k, nvalid))
+                    flag_health(a.health, MHD_HEALTH_STALL);
+            } else if constexpr (GROUPED) {
                 const int ru = 5 * nvalid, rb = 3 * (nvalid + 1);
                 const int pb2 = nib(f.pb, 2);
                 // Groups of 4 rows (cells i0 .. i0+3 of the tile's pencils, N is a
@@ -476,7 +484,10 @@ __device__ __forceinline__ void fluidx_tile_reg(const FluidxArgs &a, long long t
             }
         }
     } else {
-        if constexpr (GROUPED) {
+        if constexpr (TMA) {
+            float *raw = txr_raw(smem, fxr_smem_floats(N, ppc, true));
+            tma_rows_writeback<N>(f, *tm, US, PS, CS, raw, j0, k, nvalid);
+        } else if constexpr (GROUPED) {
             // groups of 4 rows: a row is ru = 5*nvalid consecutive floats at
             // u_out + (row cell + j0)*5; the 4*ru <= 160 floats of a group take
             // five passes of a warp, each lane with fixed (row, pencil, component)

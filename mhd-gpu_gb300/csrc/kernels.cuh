@@ -75,6 +75,9 @@ bool frame_supported(const Frame &f);
 PencilCfg pencil_cfg(int kclass, int n, bool rows = false);
 PencilCfg rows_pick(int kclass, int n);
 int math_mode();
+// how row-staged pencils are moved (MHD_STAGING_TMA or MHD_STAGING_CPASYNC;
+// the calling host thread's setting)
+int row_staging();
 cudaError_t launch_fluidx(const FluidxArgs &a, const PencilCfg &cfg, int math, cudaStream_t s);
 cudaError_t launch_fluidx_faithful(const FluidxArgs &a, const PencilCfg &cfg, cudaStream_t s);
 cudaError_t launch_fluidx_fast(const FluidxArgs &a, const PencilCfg &cfg, cudaStream_t s);

@@ -19,7 +19,9 @@ namespace mhd {
 
 static std::mutex g_tile_mutex;
 static std::map<std::pair<int, int>, PencilCfg> g_tiles;
-static std::atomic<int> g_math{MHD_MATH_FAITHFUL};
+// per host thread: a setting made on one thread changes only that thread's launches
+static thread_local int g_math = MHD_MATH_FAITHFUL;
+static thread_local int g_staging = MHD_STAGING_TMA;
 
 // Pencils across memory are staged in rows of PPC cells, so they want many
 // pencils per CTA (a row of 8 cells is 160 bytes of u).  256-cell pencils take
@@ -49,7 +51,8 @@ PencilCfg pencil_cfg(int kclass, int n, bool rows)
     return kclass == MHD_KCLASS_ADVECT ? advect_pick(n) : fluidx_pick(n);
 }
 
-int math_mode() { return g_math.load(std::memory_order_relaxed); }
+int math_mode() { return g_math; }
+int row_staging() { return g_staging; }
 
 // synthetic state for timing: rho = 1 + small ripple, weak flow, B ~ (1, .1, .2)
 __global__ void tune_fill_kernel(float *u, float *b, long long ncell)
@@ -80,7 +83,20 @@ int mhdgpu_set_math(int mode)
         set_last_error("mhdgpu_set_math: unknown mode");
         return -1;
     }
-    return g_math.exchange(mode);
+    const int prev = g_math;
+    g_math = mode;
+    return prev;
+}
+
+int mhdgpu_set_row_staging(int mode)
+{
+    if (mode != MHD_STAGING_TMA && mode != MHD_STAGING_CPASYNC) {
+        set_last_error("mhdgpu_set_row_staging: unknown mode");
+        return -1;
+    }
+    const int prev = g_staging;
+    g_staging = mode;
+    return prev;
 }
 
 static bool tile_class_ok(int kclass)

@@ -38,7 +38,7 @@ EXPORTS = [
     "mhdgpu_copy_matrix", "mhdgpu_step_workspace_bytes", "mhdgpu_step", "mhdgpu_advance",
     "mhdgpu_step_fused_workspace_bytes", "mhdgpu_step_fused",
     "mhdgpu_run_host", "mhdgpu_release_host_cache", "mhdgpu_resolve_path", "mhdgpu_path_workspace_bytes",
-    "mhdgpu_set_math", "mhdgpu_set_tile", "mhdgpu_get_tile",
+    "mhdgpu_set_math", "mhdgpu_set_row_staging", "mhdgpu_set_tile", "mhdgpu_get_tile",
     "mhdgpu_autotune", "mhdgpu_profiler_create", "mhdgpu_profiler_destroy",
     "mhdgpu_profiler_attach", "mhdgpu_profiler_reset", "mhdgpu_profiler_summary",
     "mhdgpu_diagnostics_scratch_bytes", "mhdgpu_diagnostics",
@@ -101,6 +101,7 @@ def lib() -> C.CDLL:
             "mhdgpu_run_host": (I, [P, P, I, I, I, D, I, P, F, I, P, P, I]),
             "mhdgpu_release_host_cache": (I, []),
             "mhdgpu_set_math": (I, [I]),
+            "mhdgpu_set_row_staging": (I, [I]),
             "mhdgpu_set_tile": (I, [I, I, I, I, I]),
             "mhdgpu_get_tile": (I, [I, I, P, P, P]),
             "mhdgpu_autotune": (I, [I, I, I, I]),
@@ -275,6 +276,19 @@ MHD_MATH_FP64P = 2
 def set_math(mode: int) -> int:
     """Select the arithmetic policy of the pencil kernels; returns the previous one."""
     prev = lib().mhdgpu_set_math(int(mode))
+    if prev < 0:
+        raise MhdError(MHD_ERR_ARG, lib().mhdgpu_last_error().decode())
+    return prev
+
+
+MHD_STAGING_TMA = 0
+MHD_STAGING_CPASYNC = 1
+
+
+def set_row_staging(mode: int) -> int:
+    """How the transpose-free step moves its y/z pencils (MHD_STAGING_TMA or
+    MHD_STAGING_CPASYNC; the calling thread's setting); returns the previous one."""
+    prev = lib().mhdgpu_set_row_staging(int(mode))
     if prev < 0:
         raise MhdError(MHD_ERR_ARG, lib().mhdgpu_last_error().decode())
     return prev
