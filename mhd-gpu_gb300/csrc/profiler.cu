@@ -9,6 +9,8 @@
 #include <cuda_runtime.h>
 #include <stdio.h>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include <vector>
 
 #include "mhdgpu.h"
@@ -43,6 +45,15 @@ void prof_end(int slot, cudaStream_t s)
     if (!p || slot < 0) return;
     cudaEventRecord(p->recs[slot].b, s);
 }
+
+void nvtx_push(int kclass)
+{
+    static const char *const names[] = {"mhdgpu fluidx", "mhdgpu advectbyzx", "mhdgpu transpose",
+                                        "mhdgpu cfl", "mhdgpu batch sweep"};
+    nvtxRangePushA(kclass >= 0 && kclass < 5 ? names[kclass] : "mhdgpu");
+}
+
+void nvtx_pop() { nvtxRangePop(); }
 
 }  // namespace mhd
 

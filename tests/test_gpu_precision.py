@@ -222,3 +222,64 @@ def test_alfven_diag_128_fp32_vs_fp64_study(gpu, oracle_lib):
     err = _alfven_vs_fp64(gpu, oracle_lib, 128, 200, oblique=True, threads=os.cpu_count())
     print("ALFVEN128_STUDY", err)
     assert all(np.isfinite(v) for v in err.values())
+
+
+def restrict2(u, b, n):
+    """2x2x2 restriction of an n^3 state to (n/2)^3 in float64: cell averages of
+    u, and face averages of b (each coarse left face is the mean of the four
+    fine faces it covers), which keeps the discrete div B of the fine field."""
+    h = n // 2
+    uu = np.asarray(u, dtype=np.float64).reshape(h, 2, h, 2, h, 2, 5).mean(axis=(1, 3, 5))
+    bb = np.asarray(b, dtype=np.float64).reshape(h, 2, h, 2, h, 2, 3)
+    bx = bb[:, :, :, :, :, 0, 0].mean(axis=(1, 3))     # fine x-face 2I, averaged over j, k pairs
+    by = bb[:, :, :, 0, :, :, 1].mean(axis=(1, 4))     # fine y-face 2J, averaged over k, i pairs
+    bz = bb[:, 0, :, :, :, :, 2].mean(axis=(2, 4))     # fine z-face 2K, averaged over j, i pairs
+    return uu.reshape(-1), np.stack([bx, by, bz], axis=-1).reshape(-1)
+
+
+@pytest.mark.slow
+@pytest.mark.skipif(not SLOW, reason="full-size study: set MHDGPU_SLOW=1")
+def test_turbulence_512_against_fp64_256_by_restriction(gpu, oracle_lib):
+    """Config 3 as stated: the 512^3 turbulent start (k^-2 velocity at rms Mach
+    0.5, k^-3 potential, mean field 0.3, rho = p = 1), 50 FP32 steps on the GPU,
+    against an FP64 run of the same solver at 256^3 from the 2x2x2 restriction
+    of the same initial state, run to the same physical time (the 256^3 grid's
+    solver time is half the 512^3 one's: the solver counts time in cells).
+    Per-field error of the restricted 512^3 FP32 state; beside it, the FP32 run
+    at 256^3 against the same FP64 run (the same-resolution precision error),
+    so the part of the first that is resolution rather than precision shows."""
+    import json
+    import ics
+    n, h = 512, 256
+    u, b = ics.turbulence(n, seed=7, mach=0.5, b_mean=0.3)
+    gu, gb, dts, clk, d0, d1 = gpu_run(gpu, u, b, (n, n, n), 50, 0.7, gpu.MHD_MATH_FAITHFUL,
+                                       path=gpu.MHD_PATH_AUTO)
+    t512 = float(clk.t)
+    ru, rb = restrict2(gu, gb, n)
+    cu, cb = restrict2(u, b, n)
+    del u, b, gu, gb
+    # FP64 oracle at 256^3 to t512 / 2 (its own CFL steps)
+    O64 = oracle_lib.oracle("f64")
+    oracle_lib.set_threads(os.cpu_count())
+    uu, bb = cu.copy(), cb.copy()
+    steps64, t64, _ = O64.run(uu, bb, h, h, h, cfl_number=0.7, tf=t512 / 2, max_steps=int(clk.iter))
+    # FP32 GPU at 256^3 from the same restricted start, to the same time
+    import torch
+    du, db = dev(cu.astype(np.float32)), dev(cb.astype(np.float32))
+    work = torch.empty(gpu.step_workspace_bytes(h, h, h, gpu.MHD_PATH_AUTO), dtype=torch.uint8, device="cuda")
+    clock = gpu.new_clock()
+    gpu.advance(du, db, h, h, h, int(clk.iter), 0.7, 0, float(np.float32(t512 / 2)), clock, None, work,
+                gpu.MHD_PATH_AUTO)   # ~half the steps reach tf; the rest take dt = 0
+    c256 = gpu.read_clock(clock)
+    fu, fb = host(du), host(db)
+    rec = {"t512": t512, "steps512": int(clk.iter), "t256_fp64": float(t64), "steps256_fp64": int(steps64),
+           "t256_fp32": float(c256.t), "steps256_fp32": int(c256.iter),
+           "fp32_512_restricted_vs_fp64_256": dict(zip(U_FIELDS + B_FIELDS,
+                                                       field_errors(ru, uu, 5) + field_errors(rb, bb, 3))),
+           "fp32_256_vs_fp64_256": dict(zip(U_FIELDS + B_FIELDS,
+                                            field_errors(fu, uu, 5) + field_errors(fb, bb, 3))),
+           "energy_drift_512": abs(d1["energy"] - d0["energy"]) / abs(d0["energy"]),
+           "max_div_b_512": d1["max_div_b"], "health_512": int(clk.health)}
+    print("CONFIG3_STUDY", json.dumps(rec))
+    assert clk.health & (gpu.MHD_HEALTH_NONFINITE | gpu.MHD_HEALTH_DENSITY) == 0
+    assert abs(c256.t / t64 - 1) < 1e-5
