@@ -260,6 +260,14 @@ int mhdgpu_set_math(int mode);
 #define MHD_STAGING_CPASYNC  1
 int mhdgpu_set_row_staging(int mode);
 
+/* Poison mode, a debugging aid: with on != 0 every entry that takes scratch
+ * (mhdgpu_advectbyzx, mhdgpu_step, mhdgpu_step_fused and so mhdgpu_advance,
+ * the batch's steps) first fills it with NaN on its stream, so a kernel that
+ * read scratch before writing it would put NaN into the state.  Results are
+ * unchanged otherwise; it costs one memset per call.  Returns the previous
+ * setting (of the calling host thread). */
+int mhdgpu_set_poison(int on);
+
 /* Team shape of a pencil kernel (kclass MHD_KCLASS_FLUIDX or
  * MHD_KCLASS_ADVECT, OR-ed with MHD_TILE_ROWS for pencils that run across
  * memory -- the y and z sweeps of mhdgpu_step_fused) for pencils of length n:

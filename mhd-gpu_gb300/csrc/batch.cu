@@ -356,6 +356,14 @@ int build_tables(mhdgpu_batch &bt)
 int launch_step(mhdgpu_batch &bt, cudaStream_t s, cudaEvent_t *ev /* 7 events or NULL */, bool first)
 {
     const int nb = bt.nbox;
+    if (poison_scratch()) {
+        // every box's flux scratch filled with NaN: a read before its write shows in the state
+        for (int i = 0; i < nb; ++i) {
+            const BoxDesc &d = bt.box[i];
+            BCU(cudaMemsetAsync(d.scr, 0xFF, 2 * sizeof(float) * (size_t)d.nx * d.ny * d.nz, s),
+                "mhdgpu_batch poison");
+        }
+    }
     {
         ProfScope ps(MHD_KCLASS_CFL, first ? 3 : 1, s);
         if (first) {

@@ -108,6 +108,9 @@ int mhdgpu_advectbyzx(float *b, const float *u, int nx, int ny, int nz, const fl
     if (st) return st;
     if (!b || !u || !d_dt || !d_scratch) return fail(MHD_ERR_ARG, "mhdgpu_advectbyzx: null pointer");
     const long long ncell = (long long)nx * ny * nz;
+    if (poison_scratch())
+        MHD_CU(cudaMemsetAsync(d_scratch, 0xFF, sizeof(float) * 2 * (size_t)ncell, (cudaStream_t)stream),
+               "mhdgpu_advectbyzx poison");
     AdvectArgs a = make_advect_args(b, u, d_dt, d_scratch, d_scratch + ncell, make_frame(nx, ny, nz));
     ProfScope ps(MHD_KCLASS_ADVECT, 2, (cudaStream_t)stream);
     MHD_CU(launch_advect(a, pencil_cfg(MHD_KCLASS_ADVECT, nx), math_mode(), (cudaStream_t)stream), "mhdgpu_advectbyzx");
@@ -233,6 +236,8 @@ static int step_plain(float *u, float *b, int nx, int ny, int nz, const float *d
         return fail(MHD_ERR_ARG, "mhdgpu_step: every axis becomes a pencil; each must be <= MHD_MAX_PENCIL");
     if (!u || !b || !d_dt || !d_work) return fail(MHD_ERR_ARG, "mhdgpu_step: null pointer");
     const size_t ncell = (size_t)nx * ny * nz;
+    if (poison_scratch())
+        MHD_CU(cudaMemsetAsync(d_work, 0xFF, mhdgpu_step_workspace_bytes(nx, ny, nz), s), "mhdgpu_step poison");
     float *u2 = (float *)d_work;
     float *b2 = u2 + 5 * ncell;
     float *scr = b2 + 3 * ncell;
@@ -297,6 +302,9 @@ static int step_fused(float *u, float *b, int nx, int ny, int nz, const float *d
         return fail(MHD_ERR_ARG, "mhdgpu_step_fused: every axis becomes a pencil; each must be <= MHD_MAX_PENCIL");
     if (!u || !b || !d_dt || !d_work) return fail(MHD_ERR_ARG, "mhdgpu_step_fused: null pointer");
     float *scr = (float *)d_work;
+    if (poison_scratch())
+        MHD_CU(cudaMemsetAsync(d_work, 0xFF, mhdgpu_step_fused_workspace_bytes(nx, ny, nz), s),
+               "mhdgpu_step_fused poison");
     const Frame fx = make_view(0, nx, ny, nz), fy = make_view(1, nx, ny, nz), fz = make_view(2, nx, ny, nz);
     if ((st = sweep_view(u, b, fx, d_dt, scr, d_health, true, s))) return st;
     if ((st = sweep_view(u, b, fy, d_dt, scr, d_health, true, s))) return st;

@@ -78,6 +78,9 @@ int math_mode();
 // how row-staged pencils are moved (MHD_STAGING_TMA or MHD_STAGING_CPASYNC;
 // the calling host thread's setting)
 int row_staging();
+// whether the entries fill their scratch with NaN before use (the calling
+// host thread's setting, mhdgpu_set_poison)
+bool poison_scratch();
 cudaError_t launch_fluidx(const FluidxArgs &a, const PencilCfg &cfg, int math, cudaStream_t s);
 cudaError_t launch_fluidx_faithful(const FluidxArgs &a, const PencilCfg &cfg, cudaStream_t s);
 cudaError_t launch_fluidx_fast(const FluidxArgs &a, const PencilCfg &cfg, cudaStream_t s);

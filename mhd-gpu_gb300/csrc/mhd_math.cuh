@@ -12,6 +12,7 @@
 #pragma once
 
 #include <math.h>
+#include <string.h>
 
 #if defined(__CUDACC__)
 #define MHD_HD __host__ __device__ __forceinline__
@@ -59,11 +60,72 @@ MHD_HD void two_prod(float a, float b, float &p, float &e)
     e = ffma(a, b, -p);
 }
 
+MHD_HD unsigned f2u(float x)
+{
+#if defined(__CUDA_ARCH__)
+    return __float_as_uint(x);
+#else
+    unsigned u;
+    memcpy(&u, &x, sizeof u);
+    return u;
+#endif
+}
+MHD_HD float u2f(unsigned u)
+{
+#if defined(__CUDA_ARCH__)
+    return __uint_as_float(u);
+#else
+    float x;
+    memcpy(&x, &u, sizeof x);
+    return x;
+#endif
+}
+
+// Rounding-boundary margin of a float result r: a threshold just below the
+// distance from r to the nearer rounding boundary beside it (half an ulp of
+// |r|, or half an ulp of the next float down when |r| is a power of two),
+// namely that distance times (1 - 2^-(K+1)).  A value v with RN(v) = r whose
+// distance |v - r| from r stays below the threshold is at least 2^-(K+1) half
+// ulps from every boundary, so any value within that much of v rounds to r as
+// well.  For |r| below 2^-100 the threshold is negative (every test against
+// it fails safe); for r = 0 it is huge.
+template <int K>
+MHD_HD float round_margin(float r)
+{
+    const unsigned b = f2u(r) & 0x7fffffffu;
+    const unsigned ones = ((1u << 23) - 1u) & ~((1u << (23 - K)) - 1u);   // 1.11..1 (K ones)
+    return u2f((((b - 1u) & 0x7f800000u) | ones) - (25u << 23));
+}
+
+// The reference's double expressions, evaluated in FP64 for the rare
+// operands whose float-float value lies too close to a rounding boundary to
+// decide the float result: exactly what the C path computes.
+MHD_HD float exact_pressure(float e, float q, float b2)
+{
+    return (float)(((double)e - (double)q / 2.0) * ((double)kGamma - 1.0) + (2.0 - (double)kGamma) * (double)b2 / 2.0);
+}
+MHD_HD float exact_quotient(float ph, float pl, float s)
+{
+    return (float)(((double)ph + (double)pl) / (double)s);
+}
+MHD_HD float exact_speed(float x, float a)
+{
+    return (float)((double)x + sqrt((double)a));
+}
+MHD_HD float exact_cfl_speed(float v, float b2, float gp, float r)
+{
+    return (float)((double)v + sqrt(fabs((double)b2 * 2.0 + (double)gp) / (double)r));
+}
+
 // Total pressure of one cell,
 //   ps = (E - |m|^2/rho/2)(gamma-1) + (2-gamma)|B|^2/2,
 // with q = |m|^2/rho and B2 = |B|^2 already rounded to float.  The reference
-// forms the whole expression in double (Heterogeneous_MHD/C/mhdflux.c:18,
-// calcfl.c:50) and rounds once; this forms it in float-float.
+// forms the whole expression in double (Heterogeneous_MHD/C/mhdflux.c:28,
+// calcfl.c:50) and rounds once to float.  Here it is formed in float-float
+// (error below 2^-46 of ps when E >= q/2, as in any physical cell); where
+// that value lies within 2^-15 half-ulps of a float rounding boundary, or E <
+// q/2, the double expression itself decides (exact_pressure), so the result
+// is the reference's float in every case.
 MHD_HD float total_pressure(float e, float q, float b2)
 {
     float ah, al;
@@ -75,20 +137,11 @@ MHD_HD float total_pressure(float e, float q, float b2)
     two_prod(b2, kTwoMGammaHalf, mh, ml);
     float sh, sl;
     two_sum(ph, mh, sh, sl);
-    return fadd(sh, fadd(sl, fadd(pl, ml)));
-}
-
-// round_to_float(x + sqrt(a)) with the sum and the root formed in double
-// (the reference calls the double libm sqrt and adds in double,
-// Heterogeneous_MHD/C/mhdflux.c:45, calcfl.c:54).  a >= 0, x >= 0.
-MHD_HD float add_sqrt(float x, float a)
-{
-    float zh = fsqrt(a);
-    float zl = 0.0f;
-    if (zh > 0.0f) zl = fdiv_approx(ffma(-zh, zh, a), 2.0f * zh);
-    float sh, sl;
-    two_sum(x, zh, sh, sl);
-    return fadd(sh, fadd(sl, zl));
+    const float t = fadd(sl, fadd(pl, ml));
+    const float r = fadd(sh, t);
+    const float d = fadd(fsub(sh, r), t);   // the value's distance from r
+    if (fabsf(d) > round_margin<14>(r) || ah < 0.0f) return exact_pressure(e, q, b2);
+    return r;
 }
 
 // ---------------------------------------------------------------------------
@@ -124,7 +177,12 @@ MHD_HD float rcp_rn(float d) { volatile float r = 1.0f / d; return r; }
 //    the IEEE quotient RN(a/d) for normal operands;
 //  - slope(X, Y) is the van Leer limiter 2ab/(a+b) of a = X/2, b = Y/2, i.e.
 //    XY/(X+Y), with the exact product XY as the reference's double numerator
-//    (Heterogeneous_MHD/C/tvd1.c:78, tvdb.c:75) and one correction step.
+//    (Heterogeneous_MHD/C/tvd1.c:78, tvdb.c:75) and one correction step from
+//    the approximate reciprocal: error below 2^-18 half-ulps of the result.
+//    The reference's RN_f(RN_d(XY/S)) equals RN_f(XY/S) (XY/S is a multiple of
+//    2^-49 of itself away from every float midpoint or on one), so where the
+//    corrected quotient lies within 2^-15 half-ulps of a boundary the double
+//    quotient decides (exact_quotient) and the result is the reference's.
 struct Faithful {
     MHD_HD static float mul(float a, float b) { return fmul(a, b); }
     MHD_HD static float add(float a, float b) { return fadd(a, b); }
@@ -150,7 +208,9 @@ struct Faithful {
         const float y = rcp_approx(s);
         const float q0 = fmul(ph, y);
         const float e = fadd(ffma(-q0, s, ph), pl);
-        const float q = ffma(e, y, q0);
+        float q = ffma(e, y, q0);
+        const float d = ffma(e, y, fsub(q0, q));   // q0 + e y - q (q0 - q is exact)
+        if (fabsf(d) > round_margin<14>(q) && ph > 0.0f) q = exact_quotient(ph, pl, s);
         return (ph > 0.0f) ? q : 0.0f;
     }
     MHD_HD static float pressure(float e, float q, float b2) { return total_pressure(e, q, b2); }
@@ -163,8 +223,12 @@ struct Faithful {
         ps = pressure(u[4], divy(s2, u[0], yr), b2);
         p = fsub(ps, 0.5f * b2);
     }
-    // RN(x + sqrt(a)) with the root in float-float: zh ~ sqrt(a) from the
-    // hardware rsqrt, zl = (a - zh^2)/(2 zh) with the exact FMA residual.
+    // RN(x + sqrt(a)) as the reference forms it (the root and the sum in
+    // double, Heterogeneous_MHD/C/mhdflux.c:45): the root in float-float, zh
+    // ~ sqrt(a) from the hardware rsqrt, zl = (a - zh^2)/(2 zh) with the FMA
+    // residual, summed with x by Fast2Sum (error below 2^-16 half-ulps of the
+    // result); within 2^-13 half-ulps of a rounding boundary the double
+    // expression decides (exact_speed).
     MHD_HD static float speed(float x, float a)
     {
         if (!(a > 0.0f)) return x;
@@ -174,7 +238,11 @@ struct Faithful {
         const float hi = fmaxf(x, zh), lo = fminf(x, zh);
         const float sh = fadd(hi, lo);
         const float sl = fsub(lo, fsub(sh, hi));          // Fast2Sum, |hi| >= |lo|
-        return fadd(sh, fadd(sl, zl));
+        const float t = fadd(sl, zl);
+        const float res = fadd(sh, t);
+        const float d = fadd(fsub(sh, res), t);
+        if (fabsf(d) > round_margin<12>(res)) return exact_speed(x, a);
+        return res;
     }
 };
 
@@ -292,7 +360,12 @@ MHD_HD float cfl_speed_c(const float u[5], const float b[3])
     if (zh > 0.0f) zl = fdiv_approx(fadd(ffma(-zh, zh, yh), yl), 2.0f * zh);
     float sh, sl;
     two_sum(v, zh, sh, sl);
-    return fadd(sh, fadd(sl, zl));
+    const float t = fadd(sl, zl);
+    const float res = fadd(sh, t);
+    const float d = fadd(fsub(sh, res), t);
+    // within 2^-11 half-ulps of a rounding boundary the double expression decides
+    if (fabsf(d) > round_margin<10>(res)) return exact_cfl_speed(v, b2, gp, r);
+    return res;
 }
 
 // Release 0.2 CFL fast speed with cell-centred B (OpenMP/mhd.f90:108-120),

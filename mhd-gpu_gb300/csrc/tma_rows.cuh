@@ -68,12 +68,18 @@ __device__ __forceinline__ bool tma_rows_stage(const Frame &f, const RowMaps &mp
     }
     bool ok = mbar_wait(bar, 0);
     if (!ok) ok = mbar_wait(bar, 0);   // give the copies a second bounded wait before reading
-    // u: [i][5P] rows (stored components) -> US[q][frame component][i]
+    // u: [i][5P] rows (stored components) -> US[q][frame component][i].  A
+    // warp takes one 16-byte column w of 32 consecutive rows: lane l reads
+    // row i0+l and writes its four floats to four component rows, so
+    // consecutive lanes write consecutive banks.
     {
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
         const float4 *R4 = reinterpret_cast<const float4 *>(RU);
-        for (int h = threadIdx.x; h < N * (WU / 4); h += blockDim.x) {
-            const int i = h / (WU / 4), w = h - i * (WU / 4);
-            const float4 v = R4[h];
+        constexpr int NB = (N + 31) / 32;
+        for (int pr = warp; pr < NB * (WU / 4); pr += nwarps) {
+            const int w = pr % (WU / 4), i = (pr / (WU / 4)) * 32 + lane;
+            if (i >= N) continue;
+            const float4 v = R4[i * (WU / 4) + w];
             const float e4[4] = {v.x, v.y, v.z, v.w};
 #pragma unroll
             for (int e = 0; e < 4; ++e) {
@@ -82,11 +88,13 @@ __device__ __forceinline__ bool tma_rows_stage(const Frame &f, const RowMaps &mp
             }
         }
     }
-    // b of columns j0 .. j0+nvalid -> SB[qb][3 i + frame component]
+    // b of columns j0 .. j0+P (the column after the last valid one is its
+    // periodic j+1 neighbour: column 0 when the tile ends the frame) ->
+    // SB[qb][3 i + frame component]; columns past it are spare
     {
-        const int rb = 3 * (nvalid + 1);
-        for (int h = threadIdx.x; h < N * rb; h += blockDim.x) {
-            const int i = h / rb, r = h - i * rb, qb = r / 3, s = r - 3 * qb;
+        constexpr int RBW = 3 * (P + 1);
+        for (int h = threadIdx.x; h < N * RBW; h += blockDim.x) {
+            const int i = h / RBW, r = h - i * RBW, qb = r / 3, s = r - 3 * qb;
             const float v = (wrap && qb == nvalid) ? RW[i * 4 + s] : RB[i * WB + r];
             SB[qb * BSR + 3 * i + nib(f.ib, s)] = v;
         }
@@ -94,8 +102,8 @@ __device__ __forceinline__ bool tma_rows_stage(const Frame &f, const RowMaps &mp
     // frame b(3) of plane k+1 -> SK[q][i]
     {
         const int s3 = nib(f.pb, 2);
-        for (int h = threadIdx.x; h < N * nvalid; h += blockDim.x) {
-            const int i = h / nvalid, qq = h - i * nvalid;
+        for (int h = threadIdx.x; h < N * P; h += blockDim.x) {
+            const int qq = h / N, i = h - qq * N;
             SK[qq * KS + i] = RK[i * WK + 3 * qq + s3];
         }
     }
@@ -116,15 +124,21 @@ __device__ __forceinline__ void tma_rows_writeback(const Frame &f, const RowMaps
     constexpr int WU = 5 * P;
     float4 *R4 = reinterpret_cast<float4 *>(raw);
     __syncthreads();
-    for (int h = threadIdx.x; h < N * (WU / 4); h += blockDim.x) {
-        const int i = h / (WU / 4), w = h - i * (WU / 4);
-        float e4[4];
+    {
+        // the u transpose's mapping, the other way
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+        constexpr int NB = (N + 31) / 32;
+        for (int pr = warp; pr < NB * (WU / 4); pr += nwarps) {
+            const int w = pr % (WU / 4), i = (pr / (WU / 4)) * 32 + lane;
+            if (i >= N) continue;
+            float e4[4];
 #pragma unroll
-        for (int e = 0; e < 4; ++e) {
-            const int idx = 4 * w + e, qq = idx / 5, s = idx - 5 * qq;
-            e4[e] = qq < nvalid ? US[qq * PS + nib(f.iu, s) * CS + i] : 0.0f;
+            for (int e = 0; e < 4; ++e) {
+                const int idx = 4 * w + e, qq = idx / 5, s = idx - 5 * qq;
+                e4[e] = qq < nvalid ? US[qq * PS + nib(f.iu, s) * CS + i] : 0.0f;
+            }
+            R4[i * (WU / 4) + w] = make_float4(e4[0], e4[1], e4[2], e4[3]);
         }
-        R4[h] = make_float4(e4[0], e4[1], e4[2], e4[3]);
     }
     fence_proxy_async_smem();
     __syncthreads();

@@ -22,6 +22,7 @@ static std::map<std::pair<int, int>, PencilCfg> g_tiles;
 // per host thread: a setting made on one thread changes only that thread's launches
 static thread_local int g_math = MHD_MATH_FAITHFUL;
 static thread_local int g_staging = MHD_STAGING_TMA;
+static thread_local int g_poison = 0;
 
 // Pencils across memory are staged in rows of PPC cells, so they want many
 // pencils per CTA (a row of 8 cells is 160 bytes of u).  256-cell pencils take
@@ -53,6 +54,7 @@ PencilCfg pencil_cfg(int kclass, int n, bool rows)
 
 int math_mode() { return g_math; }
 int row_staging() { return g_staging; }
+bool poison_scratch() { return g_poison != 0; }
 
 // synthetic state for timing: rho = 1 + small ripple, weak flow, B ~ (1, .1, .2)
 __global__ void tune_fill_kernel(float *u, float *b, long long ncell)
@@ -85,6 +87,13 @@ int mhdgpu_set_math(int mode)
     }
     const int prev = g_math;
     g_math = mode;
+    return prev;
+}
+
+int mhdgpu_set_poison(int on)
+{
+    const int prev = g_poison;
+    g_poison = on ? 1 : 0;
     return prev;
 }
 

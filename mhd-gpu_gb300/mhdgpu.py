@@ -38,7 +38,7 @@ EXPORTS = [
     "mhdgpu_copy_matrix", "mhdgpu_step_workspace_bytes", "mhdgpu_step", "mhdgpu_advance",
     "mhdgpu_step_fused_workspace_bytes", "mhdgpu_step_fused",
     "mhdgpu_run_host", "mhdgpu_release_host_cache", "mhdgpu_resolve_path", "mhdgpu_path_workspace_bytes",
-    "mhdgpu_set_math", "mhdgpu_set_row_staging", "mhdgpu_set_tile", "mhdgpu_get_tile",
+    "mhdgpu_set_math", "mhdgpu_set_row_staging", "mhdgpu_set_poison", "mhdgpu_set_tile", "mhdgpu_get_tile",
     "mhdgpu_autotune", "mhdgpu_profiler_create", "mhdgpu_profiler_destroy",
     "mhdgpu_profiler_attach", "mhdgpu_profiler_reset", "mhdgpu_profiler_summary",
     "mhdgpu_diagnostics_scratch_bytes", "mhdgpu_diagnostics",
@@ -102,6 +102,7 @@ def lib() -> C.CDLL:
             "mhdgpu_release_host_cache": (I, []),
             "mhdgpu_set_math": (I, [I]),
             "mhdgpu_set_row_staging": (I, [I]),
+            "mhdgpu_set_poison": (I, [I]),
             "mhdgpu_set_tile": (I, [I, I, I, I, I]),
             "mhdgpu_get_tile": (I, [I, I, P, P, P]),
             "mhdgpu_autotune": (I, [I, I, I, I]),
@@ -292,6 +293,12 @@ def set_row_staging(mode: int) -> int:
     if prev < 0:
         raise MhdError(MHD_ERR_ARG, lib().mhdgpu_last_error().decode())
     return prev
+
+
+def set_poison(on: bool) -> bool:
+    """Fill every entry's scratch with NaN before use (a debugging aid; the
+    calling thread's setting); returns the previous setting."""
+    return bool(lib().mhdgpu_set_poison(1 if on else 0))
 
 
 MHD_TILE_ROWS = 16
