@@ -97,22 +97,47 @@ MHD_HD float round_margin(float r)
     return u2f((((b - 1u) & 0x7f800000u) | ones) - (25u << 23));
 }
 
+// A branch taken by a lane only in rare cases: the warp enters it only when
+// some active lane needs it, so the common path never issues (even
+// predicated) the instructions behind it.
+#if defined(__CUDA_ARCH__)
+#define MHD_RARE(cond) (__any_sync(__activemask(), (cond)))
+#else
+#define MHD_RARE(cond) (cond)
+#endif
+
 // The reference's double expressions, evaluated in FP64 for the rare
 // operands whose float-float value lies too close to a rounding boundary to
 // decide the float result: exactly what the C path computes.
-MHD_HD float exact_pressure(float e, float q, float b2)
+MHD_HD
+#if defined(__CUDA_ARCH__)
+__noinline__
+#endif
+float exact_pressure(float e, float q, float b2)
 {
     return (float)(((double)e - (double)q / 2.0) * ((double)kGamma - 1.0) + (2.0 - (double)kGamma) * (double)b2 / 2.0);
 }
-MHD_HD float exact_quotient(float ph, float pl, float s)
+MHD_HD
+#if defined(__CUDA_ARCH__)
+__noinline__
+#endif
+float exact_quotient(float ph, float pl, float s)
 {
     return (float)(((double)ph + (double)pl) / (double)s);
 }
-MHD_HD float exact_speed(float x, float a)
+MHD_HD
+#if defined(__CUDA_ARCH__)
+__noinline__
+#endif
+float exact_speed(float x, float a)
 {
     return (float)((double)x + sqrt((double)a));
 }
-MHD_HD float exact_cfl_speed(float v, float b2, float gp, float r)
+MHD_HD
+#if defined(__CUDA_ARCH__)
+__noinline__
+#endif
+float exact_cfl_speed(float v, float b2, float gp, float r)
 {
     return (float)((double)v + sqrt(fabs((double)b2 * 2.0 + (double)gp) / (double)r));
 }
@@ -140,7 +165,8 @@ MHD_HD float total_pressure(float e, float q, float b2)
     const float t = fadd(sl, fadd(pl, ml));
     const float r = fadd(sh, t);
     const float d = fadd(fsub(sh, r), t);   // the value's distance from r
-    if (fabsf(d) > round_margin<14>(r) || ah < 0.0f) return exact_pressure(e, q, b2);
+    const bool near = fabsf(d) > round_margin<14>(r) || ah < 0.0f;
+    if (MHD_RARE(near)) return near ? exact_pressure(e, q, b2) : r;
     return r;
 }
 
@@ -210,7 +236,8 @@ struct Faithful {
         const float e = fadd(ffma(-q0, s, ph), pl);
         float q = ffma(e, y, q0);
         const float d = ffma(e, y, fsub(q0, q));   // q0 + e y - q (q0 - q is exact)
-        if (fabsf(d) > round_margin<14>(q) && ph > 0.0f) q = exact_quotient(ph, pl, s);
+        const bool near = fabsf(d) > round_margin<14>(q) && ph > 0.0f;
+        if (MHD_RARE(near)) q = near ? exact_quotient(ph, pl, s) : q;
         return (ph > 0.0f) ? q : 0.0f;
     }
     MHD_HD static float pressure(float e, float q, float b2) { return total_pressure(e, q, b2); }
@@ -241,7 +268,8 @@ struct Faithful {
         const float t = fadd(sl, zl);
         const float res = fadd(sh, t);
         const float d = fadd(fsub(sh, res), t);
-        if (fabsf(d) > round_margin<12>(res)) return exact_speed(x, a);
+        const bool near = fabsf(d) > round_margin<12>(res);
+        if (MHD_RARE(near)) return near ? exact_speed(x, a) : res;
         return res;
     }
 };
@@ -364,7 +392,8 @@ MHD_HD float cfl_speed_c(const float u[5], const float b[3])
     const float res = fadd(sh, t);
     const float d = fadd(fsub(sh, res), t);
     // within 2^-11 half-ulps of a rounding boundary the double expression decides
-    if (fabsf(d) > round_margin<10>(res)) return exact_cfl_speed(v, b2, gp, r);
+    const bool near = fabsf(d) > round_margin<10>(res);
+    if (MHD_RARE(near)) return near ? exact_cfl_speed(v, b2, gp, r) : res;
     return res;
 }
 

@@ -283,3 +283,40 @@ def test_turbulence_512_against_fp64_256_by_restriction(gpu, oracle_lib):
     print("CONFIG3_STUDY", json.dumps(rec))
     assert clk.health & (gpu.MHD_HEALTH_NONFINITE | gpu.MHD_HEALTH_DENSITY) == 0
     assert abs(c256.t / t64 - 1) < 1e-5
+
+
+BLAST_RECORD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "blast256_f64.json")
+
+
+@pytest.mark.skipif(not os.path.exists(BLAST_RECORD), reason="FP64 blast record not generated")
+def test_lowbeta_blast_256_against_fp64_record(gpu):
+    """Config 5 at its own size (256^3 low-beta blast, 300 steps at CFL 0.7)
+    in FP32 and FP32 + FP64 pressure recovery on the GPU, against the
+    diagnostics of the FP64 oracle's run of the same configuration
+    (tests/golden/blast256_f64.json, made by gen_blast256_f64.py): both
+    policies stay finite with rho > 0, conserve mass and energy to FP32
+    round-off, keep div B at round-off of |B| = 10, and lose positivity in the
+    same cells as FP64 does (the scheme's own loss: the count of cells with
+    p <= 0 within 3% of the FP64 run's, the minimum within a factor of 1.5)."""
+    import json
+    import ics
+    rec = json.load(open(BLAST_RECORD))
+    n = rec["config"]["n"]
+    u, b = ics.blast(n)
+    out = {}
+    for name, math in (("fp32", gpu.MHD_MATH_FAITHFUL), ("fp64_pressure", gpu.MHD_MATH_FP64P)):
+        gu, gb, dts, clk, d0, d1 = gpu_run(gpu, u, b, (n, n, n), rec["config"]["steps"], rec["config"]["cfl"],
+                                           math, path=gpu.MHD_PATH_AUTO)
+        out[name] = {"health": int(clk.health), "t": float(clk.t), "min_p": d1["min_p"],
+                     "cells_p_nonpositive": d1["cells_p_nonpositive"],
+                     "energy_drift": abs(d1["energy"] - d0["energy"]) / abs(d0["energy"]),
+                     "mass_drift": abs(d1["mass"] - d0["mass"]) / abs(d0["mass"]),
+                     "max_div_b": d1["max_div_b"]}
+    print("BLAST256", json.dumps({"gpu": out, "fp64_record": rec["final"], "fp64_t": rec["t_end"]}))
+    ref = rec["final"]
+    for name, r in out.items():
+        assert r["health"] & (gpu.MHD_HEALTH_NONFINITE | gpu.MHD_HEALTH_DENSITY) == 0, name
+        assert r["energy_drift"] < 1e-6 and r["mass_drift"] < 1e-6, (name, r)
+        assert r["max_div_b"] < 2e-4, (name, r)
+        assert abs(r["cells_p_nonpositive"] / ref["cells_p_nonpositive"] - 1) < 0.03, (name, r, ref)
+        assert ref["min_p"] * 1.5 < r["min_p"] < ref["min_p"] / 1.5, (name, r, ref)
