@@ -81,30 +81,19 @@ MHD_HD float u2f(unsigned u)
 #endif
 }
 
-// Rounding-boundary margin of a float result r: a threshold just below the
-// distance from r to the nearer rounding boundary beside it (half an ulp of
-// |r|, or half an ulp of the next float down when |r| is a power of two),
-// namely that distance times (1 - 2^-(K+1)).  A value v with RN(v) = r whose
-// distance |v - r| from r stays below the threshold is at least 2^-(K+1) half
-// ulps from every boundary, so any value within that much of v rounds to r as
-// well.  For |r| below 2^-100 the threshold is negative (every test against
-// it fails safe); for r = 0 it is huge.
+// Whether a float-float value v = r + d (r = RN(v), d the small remainder)
+// lies within 2^-K |d| of a float rounding boundary: v nudged by +-2^-K of
+// its remainder rounds to two different floats.  Where it does not, every
+// value within that distance of v -- the exact value included, when the
+// float-float error is below it -- rounds to r.  Pure FP32: two FMAs and a
+// compare, and a power-of-two r (whose lower rounding interval is half as
+// wide) needs no special case.
 template <int K>
-MHD_HD float round_margin(float r)
+MHD_HD bool near_boundary(float r, float d)
 {
-    const unsigned b = f2u(r) & 0x7fffffffu;
-    const unsigned ones = ((1u << 23) - 1u) & ~((1u << (23 - K)) - 1u);   // 1.11..1 (K ones)
-    return u2f((((b - 1u) & 0x7f800000u) | ones) - (25u << 23));
+    const float up = 1.0f + 1.0f / (float)(1 << K), dn = 1.0f - 1.0f / (float)(1 << K);
+    return ffma(d, up, r) != ffma(d, dn, r);
 }
-
-// A branch taken by a lane only in rare cases: the warp enters it only when
-// some active lane needs it, so the common path never issues (even
-// predicated) the instructions behind it.
-#if defined(__CUDA_ARCH__)
-#define MHD_RARE(cond) (__any_sync(__activemask(), (cond)))
-#else
-#define MHD_RARE(cond) (cond)
-#endif
 
 // The reference's double expressions, evaluated in FP64 for the rare
 // operands whose float-float value lies too close to a rounding boundary to
@@ -148,9 +137,9 @@ float exact_cfl_speed(float v, float b2, float gp, float r)
 // forms the whole expression in double (Heterogeneous_MHD/C/mhdflux.c:28,
 // calcfl.c:50) and rounds once to float.  Here it is formed in float-float
 // (error below 2^-46 of ps when E >= q/2, as in any physical cell); where
-// that value lies within 2^-15 half-ulps of a float rounding boundary, or E <
-// q/2, the double expression itself decides (exact_pressure), so the result
-// is the reference's float in every case.
+// that value lies within 2^-14 of its remainder of a float rounding boundary
+// (near_boundary), or E < q/2, the double expression itself decides
+// (exact_pressure), so the result is the reference's float in every case.
 MHD_HD float total_pressure(float e, float q, float b2)
 {
     float ah, al;
@@ -165,8 +154,7 @@ MHD_HD float total_pressure(float e, float q, float b2)
     const float t = fadd(sl, fadd(pl, ml));
     const float r = fadd(sh, t);
     const float d = fadd(fsub(sh, r), t);   // the value's distance from r
-    const bool near = fabsf(d) > round_margin<14>(r) || ah < 0.0f;
-    if (MHD_RARE(near)) return near ? exact_pressure(e, q, b2) : r;
+    if (near_boundary<14>(r, d) || ah < 0.0f) return exact_pressure(e, q, b2);
     return r;
 }
 
@@ -207,7 +195,8 @@ MHD_HD float rcp_rn(float d) { volatile float r = 1.0f / d; return r; }
 //    the approximate reciprocal: error below 2^-18 half-ulps of the result.
 //    The reference's RN_f(RN_d(XY/S)) equals RN_f(XY/S) (XY/S is a multiple of
 //    2^-49 of itself away from every float midpoint or on one), so where the
-//    corrected quotient lies within 2^-15 half-ulps of a boundary the double
+//    corrected quotient lies near a boundary (near_boundary, a window of 2^-14
+//    of its remainder, i.e. of 2^-14 half-ulps where it matters) the double
 //    quotient decides (exact_quotient) and the result is the reference's.
 struct Faithful {
     MHD_HD static float mul(float a, float b) { return fmul(a, b); }
@@ -236,8 +225,7 @@ struct Faithful {
         const float e = fadd(ffma(-q0, s, ph), pl);
         float q = ffma(e, y, q0);
         const float d = ffma(e, y, fsub(q0, q));   // q0 + e y - q (q0 - q is exact)
-        const bool near = fabsf(d) > round_margin<14>(q) && ph > 0.0f;
-        if (MHD_RARE(near)) q = near ? exact_quotient(ph, pl, s) : q;
+        if (near_boundary<14>(q, d) && ph > 0.0f) q = exact_quotient(ph, pl, s);
         return (ph > 0.0f) ? q : 0.0f;
     }
     MHD_HD static float pressure(float e, float q, float b2) { return total_pressure(e, q, b2); }
@@ -254,8 +242,8 @@ struct Faithful {
     // double, Heterogeneous_MHD/C/mhdflux.c:45): the root in float-float, zh
     // ~ sqrt(a) from the hardware rsqrt, zl = (a - zh^2)/(2 zh) with the FMA
     // residual, summed with x by Fast2Sum (error below 2^-16 half-ulps of the
-    // result); within 2^-13 half-ulps of a rounding boundary the double
-    // expression decides (exact_speed).
+    // result); near a rounding boundary (a window of 2^-12 of the remainder)
+    // the double expression decides (exact_speed).
     MHD_HD static float speed(float x, float a)
     {
         if (!(a > 0.0f)) return x;
@@ -268,8 +256,7 @@ struct Faithful {
         const float t = fadd(sl, zl);
         const float res = fadd(sh, t);
         const float d = fadd(fsub(sh, res), t);
-        const bool near = fabsf(d) > round_margin<12>(res);
-        if (MHD_RARE(near)) return near ? exact_speed(x, a) : res;
+        if (near_boundary<12>(res, d)) return exact_speed(x, a);
         return res;
     }
 };
@@ -391,9 +378,8 @@ MHD_HD float cfl_speed_c(const float u[5], const float b[3])
     const float t = fadd(sl, zl);
     const float res = fadd(sh, t);
     const float d = fadd(fsub(sh, res), t);
-    // within 2^-11 half-ulps of a rounding boundary the double expression decides
-    const bool near = fabsf(d) > round_margin<10>(res);
-    if (MHD_RARE(near)) return near ? exact_cfl_speed(v, b2, gp, r) : res;
+    // near a rounding boundary (2^-10 of the remainder) the double expression decides
+    if (near_boundary<10>(res, d)) return exact_cfl_speed(v, b2, gp, r);
     return res;
 }
 
