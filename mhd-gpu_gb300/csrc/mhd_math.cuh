@@ -95,16 +95,38 @@ MHD_HD bool near_boundary(float r, float d)
     return ffma(d, up, r) != ffma(d, dn, r);
 }
 
+// Double arithmetic with one rounding per operation: the fallbacks below
+// must not be contracted into FMAs (a*b + c fused rounds once where the C
+// path rounds the product and the sum separately; on a double tie the float
+// result then differs).
+#if defined(__CUDA_ARCH__)
+MHD_HD double dmul(double a, double b) { return __dmul_rn(a, b); }
+MHD_HD double dadd(double a, double b) { return __dadd_rn(a, b); }
+MHD_HD double dsub(double a, double b) { return __dsub_rn(a, b); }
+MHD_HD double ddiv(double a, double b) { return __ddiv_rn(a, b); }
+MHD_HD double dsqrt(double a) { return __dsqrt_rn(a); }
+#else
+MHD_HD double dmul(double a, double b) { volatile double r = a * b; return r; }
+MHD_HD double dadd(double a, double b) { volatile double r = a + b; return r; }
+MHD_HD double dsub(double a, double b) { volatile double r = a - b; return r; }
+MHD_HD double ddiv(double a, double b) { volatile double r = a / b; return r; }
+MHD_HD double dsqrt(double a) { return sqrt(a); }
+#endif
+
 // The reference's double expressions, evaluated in FP64 for the rare
 // operands whose float-float value lies too close to a rounding boundary to
-// decide the float result: exactly what the C path computes.
+// decide the float result: exactly what the C path computes, operation by
+// operation.
 MHD_HD
 #if defined(__CUDA_ARCH__)
 __noinline__
 #endif
 float exact_pressure(float e, float q, float b2)
 {
-    return (float)(((double)e - (double)q / 2.0) * ((double)kGamma - 1.0) + (2.0 - (double)kGamma) * (double)b2 / 2.0);
+    // ((E - q/2.0)*(gamma - 1.0) + (2.0 - gamma)*B2/2.0), mhdflux.c:28
+    const double a = dsub((double)e, ddiv((double)q, 2.0));
+    const double m = ddiv(dmul(dsub(2.0, (double)kGamma), (double)b2), 2.0);
+    return (float)dadd(dmul(a, dsub((double)kGamma, 1.0)), m);
 }
 MHD_HD
 #if defined(__CUDA_ARCH__)
@@ -112,7 +134,7 @@ __noinline__
 #endif
 float exact_quotient(float ph, float pl, float s)
 {
-    return (float)(((double)ph + (double)pl) / (double)s);
+    return (float)ddiv(dadd((double)ph, (double)pl), (double)s);
 }
 MHD_HD
 #if defined(__CUDA_ARCH__)
@@ -120,7 +142,7 @@ __noinline__
 #endif
 float exact_speed(float x, float a)
 {
-    return (float)((double)x + sqrt((double)a));
+    return (float)dadd((double)x, dsqrt((double)a));
 }
 MHD_HD
 #if defined(__CUDA_ARCH__)
@@ -128,7 +150,8 @@ __noinline__
 #endif
 float exact_cfl_speed(float v, float b2, float gp, float r)
 {
-    return (float)((double)v + sqrt(fabs((double)b2 * 2.0 + (double)gp) / (double)r));
+    // v + sqrt(fabs(B2*2.0 + gamma p) / rho), calcfl.c:54 (fabs of the numerator only)
+    return (float)dadd((double)v, dsqrt(ddiv(fabs(dadd(dmul((double)b2, 2.0), (double)gp)), (double)r)));
 }
 
 // Total pressure of one cell,

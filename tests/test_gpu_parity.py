@@ -60,6 +60,20 @@ def test_fluidx_matches_oracle(gpu, oracle_lib, dims):
     assert bits_equal(host(du2), u)                        # input untouched
 
 
+def test_fluidx_pressure_on_a_double_tie(gpu):
+    """tests/golden/tie_pencil.npz: a cell whose total pressure the C path
+    rounds twice in double away from a tie (mhdflux.c:28).  The rare-operand
+    fallback must round the product and the sum separately, as the C path
+    does; a contracted FMA lands on the float midpoint and rounds the other
+    way.  Bit-exact, all math policies that claim the C path's rounding."""
+    z = np.load(os.path.join(GOLD, "tie_pencil.npz"))
+    nx, ny, nz = (int(x) for x in z["dims"])
+    du, db = dev(z["u"]), dev(z["b"])
+    out = dev(np.zeros_like(z["u"]))
+    gpu.fluidx(out, du, db, nx, ny, nz, scalar(np.float32(z["dt"][0])))
+    assert bits_equal(host(out), z["out"])
+
+
 @pytest.mark.parametrize("dims", SHAPES)
 def test_advectbyzx_matches_oracle(gpu, oracle_lib, dims):
     import ics

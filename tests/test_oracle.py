@@ -188,3 +188,44 @@ def test_oracle64_keeps_div_b_and_conserves_on_a_noncubic_state(oracle_lib):
     t1 = ics.totals(u, nx, ny, nz)
     assert abs(t1[0] - t0[0]) < 1e-12 * abs(t0[0])
     assert abs(t1[4] - t0[4]) < 1e-12 * abs(t0[4])
+
+
+def test_tie_pencil_fixture_is_a_double_tie(oracle_lib):
+    """The fixture of tests/golden/gen_tie_pencil.py: the oracle reproduces
+    its stored fluidx output, and cell 70's half-step total pressure is the
+    double-rounding case the fixture is kept for -- the exact value lies half
+    a double ulp above a float midpoint, the C path's RN_d(RN_d(A G) + M)
+    one ulp above it (rounds up), a fused A G + M on the midpoint (rounds to
+    even, down)."""
+    from fractions import Fraction as Fr
+    O = oracle_lib.oracle("f32")
+    z = np.load(os.path.join(GOLD, "tie_pencil.npz"))
+    nx, ny, nz = (int(x) for x in z["dims"])
+    dt = np.float32(z["dt"][0])
+    out = np.zeros_like(z["u"])
+    O.fluidx(out, z["b"].copy(), nx, ny, nz, dt, z["u"].copy(), z["b"].copy())
+    assert bits_equal(out, z["out"])
+    # cell 70 of pencil (0, 0) before the half step: u and the cell-centred b
+    f32 = np.float32
+    u = z["u"].reshape(nz, ny, nx, 5)[0, 0, 70]
+    bb = z["b"].reshape(nz, ny, nx, 3)
+    bx = f32(f32(0.5) * bb[0, 0, 70, 0]) + f32(f32(0.5) * bb[0, 0, 71, 0])
+    by = f32(f32(0.5) * bb[0, 0, 70, 1]) + f32(bb[0, 1, 70, 1] / f32(2))
+    bz = f32(f32(0.5) * bb[0, 0, 70, 2]) + f32(bb[1, 0, 70, 2] / f32(2))
+    r, m1, m2, m3, e = u
+    q = f32(f32(f32(f32(m1 * m1) + f32(m2 * m2)) + f32(m3 * m3)) / r)
+    b2 = f32(f32(f32(bx * bx) + f32(by * by)) + f32(bz * bz))
+    g = float(f32(5.0 / 3.0))
+    a = float(e) - float(q) / 2.0
+    m = (2.0 - g) * float(b2) / 2.0
+    c_path = a * (g - 1.0) + m                       # two double roundings
+    exact = Fr(a) * (Fr(g) - 1) + Fr(m)
+    assert Fr(a) == Fr(float(e)) - Fr(float(q)) / 2 and Fr(m) == (2 - Fr(g)) * Fr(float(b2)) / 2
+    lo = float(f32(c_path))
+    lo = float(np.nextafter(f32(lo), f32(0)))
+    mid = (Fr(lo) + Fr(float(f32(c_path)))) / 2
+    ulp_d = Fr(2.0 ** -52)                           # the double ulp at ps ~ 1.03
+    assert 1.0 <= c_path < 2.0
+    assert exact - mid == ulp_d / 2                  # a tie in double
+    assert Fr(c_path) - mid == ulp_d                 # the C path's double, above
+    assert float(f32(c_path)) > float(mid)           # rounds up in float
