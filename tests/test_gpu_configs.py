@@ -137,17 +137,17 @@ def _ulps(a, b):
 
 def test_ensemble64_batched_matches_oracle(gpu, oracle_lib, ensemble64):
     """The benchmark's 64-box ensemble, batched, five steps: every box against
-    the oracle run on that box alone (its own CFL and dt sequence).
+    the oracle run on that box alone (its own CFL and dt sequence), bit for
+    bit: every dt and every value of u and b.
 
     The faithful kernels form the C path's double intermediates in
-    float-float, accurate to about 2^-46 rather than exactly: on smooth states
-    (the wave boxes, configs 1 and 2) they give the C path's bits, while on a
-    turbulent state about one van Leer quotient in 3 million and one fast
-    speed in 400 thousand round the other way, and a box's dt (within 2 ulp)
-    and state drift from the oracle's in the last bits.  The bar is 2 ulp on
-    every dt and 1e-5 of the state's scale (its largest value) on every box;
-    the boxes that match bit for bit, and the worst per-field error, are
-    reported."""
+    float-float and hand the rare operands whose result lies within a narrow
+    window of a float rounding boundary to the C path's own double
+    expression, rounded operation by operation, so turbulent boxes (where
+    such operands do occur: about one van Leer quotient in 3 million, and
+    now and then a total pressure whose double evaluation ends on a tie, as
+    in tests/golden/tie_pencil.npz) match as well as the smooth wave boxes.  The per-box counts and the worst errors are printed
+    with the verdict."""
     ens = ensemble64
     assert sum(int(np.prod(e["dims"])) for e in ens) == 27246592
     boxes = [(dev(e["u"]), dev(e["b"]), e["dims"]) for e in ens]
@@ -189,8 +189,8 @@ def test_ensemble64_batched_matches_oracle(gpu, oracle_lib, ensemble64):
                          "bit_equal_by_kind": {k: f"{a}/{n}" for k, (a, n) in by_kind.items()},
                          "worst_dt_ulps": worst_ulps, "worst_error_against_state_scale": worst_scale,
                          "worst_per_field_error": worst_field})
-    assert worst_ulps <= 2
-    assert worst_scale < TOL
+    assert worst_ulps == 0
+    assert bit_equal == len(ens), (bit_equal, worst_scale, worst_field)
 
 
 def test_copy_matrix_and_compat_copies_bit_exact(gpu, oracle_lib):
