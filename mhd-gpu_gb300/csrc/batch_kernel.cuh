@@ -173,29 +173,39 @@ batch_class_kernel(const __grid_constant__ ClassWork w)
 {
     __shared__ int s_e, s_run;
     __shared__ long long s_local;
-    const long long total = w.start[3 * w.nb];
-    // thread 0 claims the next item while the CTA works on the current one
+    // the launch's prefix table (items < 2^31), items' sizes and, per (slot,
+    // box), whether this CTA has already seen the entry's dependency complete
+    __shared__ unsigned s_start[3 * kGroupBoxes + 1];
+    __shared__ int s_group[3 * kGroupBoxes];
+    __shared__ unsigned char s_ok[3 * kGroupBoxes];
+    const int ne = 3 * w.nb;
+    for (int x = threadIdx.x; x <= ne; x += blockDim.x) s_start[x] = (unsigned)w.start[x];
+    for (int x = threadIdx.x; x < ne; x += blockDim.x) {
+        s_group[x] = w.group[x];
+        s_ok[x] = 0;
+    }
+    __syncthreads();
+    const unsigned total = s_start[ne];
+    // thread 0 claims the next item while the CTA works on the current one;
+    // a CTA's claims increase, so its entry only moves forward
     unsigned it = 0;
+    int ecur = 0;
     if (threadIdx.x == 0) it = atomicAdd(w.claim, 1u);
     for (;;) {
         if (threadIdx.x == 0) {
             int e = -1, run = 0;
             long long local = 0;
-            if ((long long)it < total) {
-                int lo = 0, hi = 3 * w.nb - 1;   // last entry with start <= it
-                while (lo < hi) {
-                    const int mid = (lo + hi + 1) >> 1;
-                    if (w.start[mid] <= (long long)it) lo = mid;
-                    else hi = mid - 1;
-                }
-                e = lo;
-                local = (long long)it - w.start[e];
+            if (it < total) {
+                while (s_start[ecur + 1] <= it) ++ecur;   // last entry with start <= it
+                e = ecur;
+                local = (long long)(it - s_start[e]);
                 run = 1;
-                if (e >= w.nb) {   // wait for the box's previous phase
+                if (e >= w.nb && !s_ok[e - w.nb]) {   // wait for the box's previous phase
                     const int prev = e - w.nb;
-                    const unsigned need = (unsigned)(w.start[prev + 1] - w.start[prev]) +
+                    const unsigned need = (s_start[prev + 1] - s_start[prev]) +
                                           (prev == 0 ? w.stall_extra : 0u);
                     run = batch_wait(w.done + prev, need, w.abort, w.fa[e % w.nb].health);
+                    if (run) s_ok[prev] = 1;   // complete for good: later items skip the wait
                 }
                 it = atomicAdd(w.claim, 1u);
             }
@@ -210,7 +220,7 @@ batch_class_kernel(const __grid_constant__ ClassWork w)
             const int slot = e / w.nb, bx = e - slot * w.nb;
             const int ph = batch_phase(slot, w.fluid_first);
             const long long local = s_local;
-            const int g = w.group[e];
+            const int g = s_group[e];
             if (ph == kPhaseB1) {
                 batch_b1(w.aa[bx], local * g, g);
             } else {

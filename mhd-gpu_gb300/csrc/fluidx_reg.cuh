@@ -108,6 +108,110 @@ __device__ __forceinline__ void load_comp(const float *p, bool live, int ii, flo
     }
 }
 
+// Vector rows staging.  A tile's row i is ppc consecutive cells of the frame's
+// j axis, contiguous in memory: 20 ppc bytes of u and 12 ppc of b.  When the
+// tile is full (ppc pencils, ppc a multiple of 4) and every row starts on a
+// 16-byte boundary (the frame's strides and the arrays' addresses multiples
+// of 4 cells, resp. 16 bytes), a thread moves a quad of four pencils of one
+// row with 16-byte accesses: five vectors of u, three of b, and scatters the
+// 20 + 12 floats to their component-major places with offsets fixed by the
+// quad's position (a handful of instructions per cell, against a warp pass
+// per row of per-lane 4-byte copies otherwise).  Consecutive threads take
+// consecutive rows, so the shared-memory stores are free of bank conflicts.
+__device__ __forceinline__ bool rows_vec_ok(const Frame &f, int ppc, int nvalid, const float *u_in,
+                                            const float *u_out, const float *b)
+{
+    const uintptr_t al = reinterpret_cast<uintptr_t>(u_in) | reinterpret_cast<uintptr_t>(u_out) |
+                         reinterpret_cast<uintptr_t>(b);
+    return nvalid == ppc && (ppc & 3) == 0 && ((f.si | f.sk) & 3) == 0 && (al & 15u) == 0;
+}
+
+// one quad of u (four pencils of row i, cells j0 + 4Q ..) -> US (its rows of
+// the component-major layout at d = US + 4Q PS + i); co[s] = frame row of
+// stored component s times CS
+template <int PS>
+__device__ __forceinline__ void rows_vec_put_u(float *d, const float4 (&v)[5], const int (&co)[5])
+{
+    const float e[20] = {v[0].x, v[0].y, v[0].z, v[0].w, v[1].x, v[1].y, v[1].z, v[1].w, v[2].x, v[2].y,
+                         v[2].z, v[2].w, v[3].x, v[3].y, v[3].z, v[3].w, v[4].x, v[4].y, v[4].z, v[4].w};
+#pragma unroll
+    for (int x = 0; x < 20; ++x) d[(x / 5) * PS + co[x % 5]] = e[x];
+}
+
+template <int N>
+__device__ __forceinline__ void rows_vec_stage(const Frame &f, const float *u_in, const float *b, float *US,
+                                               float *SB, float *SK, int j0, int k, int ppc)
+{
+    constexpr int CS = N + 4, PS = 5 * CS, BSR = 3 * N + 4, KS = N + 4;
+    const long long kb = (long long)k * f.sk;
+    const int kp = (k + 1 == f.nz) ? 0 : k + 1;
+    const long long kpb = (long long)kp * f.sk;
+    const int pb2 = nib(f.pb, 2);
+    int co[5], cb[3];
+#pragma unroll
+    for (int s = 0; s < 5; ++s) co[s] = nib(f.iu, s) * CS;
+#pragma unroll
+    for (int s = 0; s < 3; ++s) cb[s] = nib(f.ib, s);
+    const int units = N * (ppc >> 2);
+    for (int un = threadIdx.x; un < units; un += blockDim.x) {
+        const int Q = un / N, i = un - Q * N;
+        const long long cell = kb + (long long)i * f.si + j0 + 4 * Q;
+        {
+            const float4 *g = reinterpret_cast<const float4 *>(u_in + cell * 5);
+            float4 v[5];
+#pragma unroll
+            for (int w = 0; w < 5; ++w) v[w] = g[w];
+            rows_vec_put_u<PS>(US + 4 * Q * PS + i, v, co);
+        }
+        {
+            const float4 *g = reinterpret_cast<const float4 *>(b + cell * 3);
+            const float4 v0 = g[0], v1 = g[1], v2 = g[2];
+            const float e[12] = {v0.x, v0.y, v0.z, v0.w, v1.x, v1.y, v1.z, v1.w, v2.x, v2.y, v2.z, v2.w};
+            float *d = SB + 4 * Q * BSR + 3 * i;
+#pragma unroll
+            for (int x = 0; x < 12; ++x) d[(x / 3) * BSR + cb[x % 3]] = e[x];
+        }
+        {
+            const float *g = b + (kpb + (long long)i * f.si + j0 + 4 * Q) * 3 + pb2;
+            float *d = SK + 4 * Q * KS + i;
+#pragma unroll
+            for (int x = 0; x < 4; ++x) d[x * KS] = g[3 * x];
+        }
+    }
+    // b of the column after the tile (column 0 when the tile ends the frame),
+    // the j+1 neighbour of its last pencil
+    int jx = j0 + ppc;
+    if (jx >= f.ny) jx -= f.ny;
+    for (int h = threadIdx.x; h < 3 * N; h += blockDim.x) {
+        const int s = h / N, i = h - s * N;
+        SB[ppc * BSR + 3 * i + cb[s]] = b[(kb + (long long)i * f.si + jx) * 3 + s];
+    }
+}
+
+// the write-back of a full tile: a thread gathers a quad of one row from the
+// component-major rows and stores its 20 floats as five 16-byte vectors
+template <int N>
+__device__ __forceinline__ void rows_vec_writeback(const Frame &f, float *u_out, const float *US, int j0, int k,
+                                                   int ppc)
+{
+    constexpr int CS = N + 4, PS = 5 * CS;
+    const long long kb = (long long)k * f.sk;
+    int co[5];
+#pragma unroll
+    for (int s = 0; s < 5; ++s) co[s] = nib(f.iu, s) * CS;
+    const int units = N * (ppc >> 2);
+    for (int un = threadIdx.x; un < units; un += blockDim.x) {
+        const int Q = un / N, i = un - Q * N;
+        const float *d = US + 4 * Q * PS + i;
+        float e[20];
+#pragma unroll
+        for (int x = 0; x < 20; ++x) e[x] = d[(x / 5) * PS + co[x % 5]];
+        float4 *g = reinterpret_cast<float4 *>(u_out + (kb + (long long)i * f.si + j0 + 4 * Q) * 5);
+#pragma unroll
+        for (int w = 0; w < 5; ++w) g[w] = make_float4(e[4 * w], e[4 * w + 1], e[4 * w + 2], e[4 * w + 3]);
+    }
+}
+
 // GROUPED: rows mode moves its rows in groups of four with per-lane offsets
 // fixed for the tile (fewer copy instructions, more registers held); the
 // single-box kernels take it, the register-capped batch kernels do not.
@@ -140,6 +244,7 @@ __device__ __forceinline__ void fluidx_tile_reg(const FluidxArgs &a, long long t
         nvalid = min(ppc, f.ny - j0);
     }
     const bool live = q < nvalid;
+    const bool vec = ROWS && !TMA && rows_vec_ok(f, ppc, nvalid, a.u_in, a.u_out, a.b);
     const int jq = ROWS ? j0 + q : (live ? (int)((p0 + q) % f.ny) : 0);
     const int kq = ROWS ? k : (live ? (int)((p0 + q) / f.ny) : 0);
 
@@ -189,6 +294,8 @@ __device__ __forceinline__ void fluidx_tile_reg(const FluidxArgs &a, long long t
                 uint64_t *bar = reinterpret_cast<uint64_t *>(raw + txr_raw_floats(N));
                 if (!tma_rows_stage<N>(f, *tm, US, PS, CS, SB, BSR, SK, KS, raw, bar, j0, k, nvalid))
                     flag_health(a.health, MHD_HEALTH_STALL);
+            } else if (vec) {
+                rows_vec_stage<N>(f, a.u_in, a.b, US, SB, SK, j0, k, ppc);
             } else if constexpr (GROUPED) {
                 const int ru = 5 * nvalid, rb = 3 * (nvalid + 1);
                 const int pb2 = nib(f.pb, 2);
@@ -487,6 +594,8 @@ __device__ __forceinline__ void fluidx_tile_reg(const FluidxArgs &a, long long t
         if constexpr (TMA) {
             float *raw = txr_raw(smem, fxr_smem_floats(N, ppc, true));
             tma_rows_writeback<N>(f, *tm, US, PS, CS, raw, j0, k, nvalid);
+        } else if (vec) {
+            rows_vec_writeback<N>(f, a.u_out, US, j0, k, ppc);
         } else if constexpr (GROUPED) {
             // groups of 4 rows: a row is ru = 5*nvalid consecutive floats at
             // u_out + (row cell + j0)*5; the 4*ru <= 160 floats of a group take
