@@ -250,12 +250,18 @@ int mhdgpu_set_math(int mode);
 
 /* How the transpose-free step moves the pencils that run across memory (its
  * y and z sweeps) between global and shared memory:
- *   MHD_STAGING_TMA (default): where the frame allows (pencils of 32, 64 or
- *     128 cells in teams of one warp, 8 per CTA, every row stride a multiple
- *     of 4 cells, 16-byte aligned arrays) the fluid tile is loaded and stored
- *     by tensor copies of the Tensor Memory Accelerator;
- *   MHD_STAGING_CPASYNC: every row is moved by 4-byte asynchronous copies.
- * Both give the same bits.  Returns the previous mode (-1 for a bad mode). */
+ *   MHD_STAGING_CPASYNC (default): a full tile of the fluid and field sweeps
+ *     (every row stride a multiple of 4 cells, 16-byte aligned arrays, pencils
+ *     per CTA a multiple of 4) is moved as 16-byte vectors of four pencils'
+ *     cells per thread; a partial tile row by row with 4-byte asynchronous
+ *     copies;
+ *   MHD_STAGING_TMA: where the frame allows (pencils of 32, 64 or 128 cells in
+ *     teams of one warp, 8 per CTA, every row stride a multiple of 4 cells,
+ *     16-byte aligned arrays) the fluid tile is loaded and stored by tensor
+ *     copies of the Tensor Memory Accelerator, with the component transpose
+ *     done in shared memory.
+ * Both give the same bits (the batch always takes the first).  Returns the
+ * previous mode (-1 for a bad mode). */
 #define MHD_STAGING_TMA      0
 #define MHD_STAGING_CPASYNC  1
 int mhdgpu_set_row_staging(int mode);
@@ -267,6 +273,28 @@ int mhdgpu_set_row_staging(int mode);
  * unchanged otherwise; it costs one memset per call.  Returns the previous
  * setting (of the calling host thread). */
 int mhdgpu_set_poison(int on);
+
+/* Debug build (lib/libmhdgpu_debug.so, build.py --debug): every shared-memory,
+ * global and halo index of the kernels is checked where it is formed; an
+ * index outside its array is skipped (a load reads 0, a store or copy does not
+ * happen) and recorded.  mhdgpu_debug_build returns 1 in that build, 0 in the
+ * release build.  mhdgpu_debug_faults synchronises the device, reports the
+ * number of faults since the last call and the first one (kind 1: an index
+ * into an array, 2: shared memory outside the launch's dynamic area, 3: a
+ * global array; the source file's number in the debug build's table and the
+ * line; the index or offset and the extent it broke) and clears the count.
+ * In the release build it reports 0 faults.  Any pointer may be NULL.
+ * File numbers: 1 fluidx_reg.cuh, 2 fluidx_kernel.cuh, 3 advect_reg.cuh,
+ * 4 advect_kernel.cuh, 5 batch_kernel.cuh, 6 transpose.cu, 7 cfl_kernel.cuh,
+ * 8 tma_rows.cuh, 9 mhd_common.cuh, 10 debug.cu.
+ * mhdgpu_debug_selftest checks index against extent in a one-thread kernel
+ * (nothing is accessed through the index) and returns in *in_bounds whether
+ * the check passed: the debug build records a failed check like any other;
+ * the release build has no checks and always reports 1. */
+int mhdgpu_debug_build(void);
+int mhdgpu_debug_faults(unsigned *count, unsigned *kind, unsigned *file, unsigned *line,
+                        long long *index, long long *extent);
+int mhdgpu_debug_selftest(long long index, long long extent, int *in_bounds);
 
 /* Team shape of a pencil kernel (kclass MHD_KCLASS_FLUIDX or
  * MHD_KCLASS_ADVECT, OR-ed with MHD_TILE_ROWS for pencils that run across

@@ -45,12 +45,21 @@ def _stale(src: str, obj: str, deps) -> bool:
     return any(os.path.getmtime(d) > t for d in [src, *deps])
 
 
-def _obj(src: str) -> str:
-    return os.path.join(BUILD, os.path.splitext(os.path.basename(src))[0] + ".o")
+# the debug build: every kernel index checked (csrc/mhd_debug.cuh); its
+# record lives in one translation unit, so the objects are relocatable
+BUILD_DEBUG = os.path.join(HERE, "_build_debug")
+LIB_DEBUG = os.path.join(LIBDIR, "libmhdgpu_debug.so")
+DEBUG_FLAGS = ["-DMHD_DEBUG", "-rdc=true"]
 
 
-def build(verbose_ptxas: bool = False, quiet: bool = True) -> str:
-    os.makedirs(BUILD, exist_ok=True)
+def _obj(src: str, bdir: str = BUILD) -> str:
+    return os.path.join(bdir, os.path.splitext(os.path.basename(src))[0] + ".o")
+
+
+def build(verbose_ptxas: bool = False, quiet: bool = True, debug: bool = False) -> str:
+    bdir, lib = (BUILD_DEBUG, LIB_DEBUG) if debug else (BUILD, LIB)
+    extra = DEBUG_FLAGS if debug else []
+    os.makedirs(bdir, exist_ok=True)
     os.makedirs(LIBDIR, exist_ok=True)
     srcs = sorted(glob.glob(os.path.join(CSRC, "*.cu")) + glob.glob(os.path.join(CSRC, "*.cpp")))
     # the heaviest translation units first, so the parallel build ends sooner
@@ -60,9 +69,9 @@ def build(verbose_ptxas: bool = False, quiet: bool = True) -> str:
     cc = nvcc()
     jobs = []
     for s in srcs:
-        o = _obj(s)
+        o = _obj(s, bdir)
         if verbose_ptxas or _stale(s, o, deps):
-            cmd = [cc, *NVFLAGS, "-c", s, "-o", o]
+            cmd = [cc, *NVFLAGS, *extra, "-c", s, "-o", o]
             if verbose_ptxas:
                 cmd += ["-Xptxas", "-v"]
             jobs.append((s, cmd))
@@ -82,14 +91,15 @@ def build(verbose_ptxas: bool = False, quiet: bool = True) -> str:
     if failed:
         msg = "\n".join(f"--- {s}\n{e}" for s, e in failed)
         raise RuntimeError("nvcc failed:\n" + msg)
-    objs = [_obj(s) for s in srcs]
-    if jobs or not os.path.exists(LIB) or any(os.path.getmtime(o) > os.path.getmtime(LIB) for o in objs):
-        cmd = [cc, *ARCH, "-shared", "-o", LIB, *objs, "-lcudart", "-Xlinker", "-Bsymbolic"]
+    objs = [_obj(s, bdir) for s in srcs]
+    if jobs or not os.path.exists(lib) or any(os.path.getmtime(o) > os.path.getmtime(lib) for o in objs):
+        cmd = [cc, *ARCH, *(["-rdc=true"] if debug else []), "-shared", "-o", lib, *objs, "-lcudart",
+               "-Xlinker", "-Bsymbolic"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("link failed:\n" + r.stderr)
-    return LIB
+    return lib
 
 
 if __name__ == "__main__":
-    print(build(verbose_ptxas="--verbose-ptxas" in sys.argv, quiet=False))
+    print(build(verbose_ptxas="--verbose-ptxas" in sys.argv, quiet=False, debug="--debug" in sys.argv))

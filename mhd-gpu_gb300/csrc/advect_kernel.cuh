@@ -25,6 +25,9 @@
 #include "advect_reg.cuh"
 #include "kernels.cuh"
 
+#undef MHD_DBG_FILE
+#define MHD_DBG_FILE 4
+
 namespace mhd {
 
 // shared floats: two alternating exchange buffers of 4 per cell and pencil,
@@ -83,6 +86,8 @@ __device__ __forceinline__ void advect_tile_team(const AdvectArgs &a, long long 
     const int rs = tm.rs();
     float *xbase = smem + (size_t)q * ax_xpen(n) + 1;
     auto X = [&](int r) { return xbase + r * rs; };
+    // value of exchange row r at cell i (-1 <= i <= n+1)
+    auto XR = [&](int r, int i) { return (MHD_IN(i + 1, rs) && MHD_SM(X(r) + i, 4)) ? X(r)[i] : 0.0f; };
 
     float vA[CPL], vB[CPL], bA[CPL], bB[CPL];
     long long base = 0;   // !ROWS: first stored cell of the pencil
@@ -98,7 +103,9 @@ __device__ __forceinline__ void advect_tile_team(const AdvectArgs &a, long long 
 #pragma unroll
         for (int m = 0; m < CPL; ++m) {
             const int c = tm.ci(m);
-            if (live && tm.valid(m)) {
+            if (live && tm.valid(m) && MHD_GM(a.u + (base + c) * 5 + 1, a.u, MHD_NU(f)) &&
+                MHD_GM(a.u + (bjm + c) * 5 + 1, a.u, MHD_NU(f)) && MHD_GM(a.u + (bkm + c) * 5 + 1, a.u, MHD_NU(f)) &&
+                MHD_GM(a.b + (base + c) * 3 + 2, a.b, MHD_NB(f))) {
                 const float r0 = a.u[(base + c) * 5 + 0], m0 = a.u[(base + c) * 5 + 1];
                 const float rj = a.u[(bjm + c) * 5 + 0], mj = a.u[(bjm + c) * 5 + 1];
                 const float rk = a.u[(bkm + c) * 5 + 0], mk = a.u[(bkm + c) * 5 + 1];
@@ -132,8 +139,8 @@ __device__ __forceinline__ void advect_tile_team(const AdvectArgs &a, long long 
         for (int i = warp; i < n; i += nwarps) {
             const long long rowc = kb + (long long)i * f.si;
             const long long rowk = kmb + (long long)i * f.si;
-            if (on2) cp_async4(&U2[i * r2 + lane], a.u + rowc * 5 + g2);
-            if (onk) {
+            if (on2 && MHD_GM(a.u + rowc * 5 + g2, a.u, MHD_NU(f))) cp_async4(&U2[i * r2 + lane], a.u + rowc * 5 + g2);
+            if (onk && MHD_GM(a.u + rowk * 5 + gk, a.u, MHD_NU(f)) && MHD_GM(a.b + rowc * 3 + gb, a.b, MHD_NB(f))) {
                 cp_async4(&UK[i * rk + lane], a.u + rowk * 5 + gk);
                 cp_async4(&BO[i * rk + lane], a.b + rowc * 3 + gb);
             }
@@ -143,9 +150,9 @@ __device__ __forceinline__ void advect_tile_team(const AdvectArgs &a, long long 
 #pragma unroll
         for (int m = 0; m < CPL; ++m) {
             const int c = tm.ci(m);
-            if (live && tm.valid(m)) {
-                const float *uo = U2 + c * r2 + 2 * (q + 1), *uj = U2 + c * r2 + 2 * q;
-                const float *uk = UK + c * rk + 2 * q, *bo = BO + c * rk + 2 * q;
+            const float *uo = U2 + c * r2 + 2 * (q + 1), *uj = U2 + c * r2 + 2 * q;
+            const float *uk = UK + c * rk + 2 * q, *bo = BO + c * rk + 2 * q;
+            if (live && tm.valid(m) && MHD_SM(uo, 8) && MHD_SM(uj, 8) && MHD_SM(uk, 8) && MHD_SM(bo, 8)) {
                 vA[m] = M::div(M::add(uj[1], uo[1]), M::add(uj[0], uo[0]));
                 vB[m] = M::div(M::add(uk[1], uo[1]), M::add(uk[0], uo[0]));
                 bA[m] = bo[0];
@@ -167,8 +174,8 @@ __device__ __forceinline__ void advect_tile_team(const AdvectArgs &a, long long 
     for (int m = 0; m < CPL; ++m) {
         if (!tm.valid(m)) continue;   // padding slots compute nothing
         const int c = tm.ci(m);
-        const float sa = M::add(X(0)[c - 1], X(0)[c + 1]);
-        const float sb = M::add(X(1)[c - 1], X(1)[c + 1]);
+        const float sa = M::add(XR(0, c - 1), XR(0, c + 1));
+        const float sb = M::add(XR(1, c - 1), XR(1, c + 1));
         gA[m] = 0.25f * M::twice_plus(vA[m], sa);
         gB[m] = 0.25f * M::twice_plus(vB[m], sb);
         tm.put(X(4), m, gA[m]);
@@ -183,10 +190,10 @@ __device__ __forceinline__ void advect_tile_team(const AdvectArgs &a, long long 
     for (int m = 0; m < CPL; ++m) {
         if (!tm.valid(m)) continue;
         const int c = tm.ci(m);
-        hA[m] = M::add(0.5f * gA[m], 0.5f * X(4)[c + 1]);
-        hB[m] = M::add(0.5f * gB[m], 0.5f * X(5)[c + 1]);
-        f1A[m] = (hA[m] > 0.0f) ? X(6)[c] : X(6)[c + 1];
-        f1B[m] = (hB[m] > 0.0f) ? X(7)[c] : X(7)[c + 1];
+        hA[m] = M::add(0.5f * gA[m], 0.5f * XR(4, c + 1));
+        hB[m] = M::add(0.5f * gB[m], 0.5f * XR(5, c + 1));
+        f1A[m] = (hA[m] > 0.0f) ? XR(6, c) : XR(6, c + 1);
+        f1B[m] = (hB[m] > 0.0f) ? XR(7, c) : XR(7, c + 1);
         tm.put(X(0), m, f1A[m]);
         tm.put(X(1), m, f1B[m]);
     }
@@ -198,8 +205,8 @@ __device__ __forceinline__ void advect_tile_team(const AdvectArgs &a, long long 
     for (int m = 0; m < CPL; ++m) {
         if (!tm.valid(m)) continue;
         const int c = tm.ci(m);
-        const float b1A = M::minus_half(bA[m], M::mul(M::sub(f1A[m], X(0)[c - 1]), dt));
-        const float b1B = M::minus_half(bB[m], M::mul(M::sub(f1B[m], X(1)[c - 1]), dt));
+        const float b1A = M::minus_half(bA[m], M::mul(M::sub(f1A[m], XR(0, c - 1)), dt));
+        const float b1B = M::minus_half(bB[m], M::mul(M::sub(f1B[m], XR(1, c - 1)), dt));
         tm.put(X(4), m, M::mul(gA[m], b1A));
         tm.put(X(5), m, M::mul(gB[m], b1B));
     }
@@ -214,17 +221,16 @@ __device__ __forceinline__ void advect_tile_team(const AdvectArgs &a, long long 
         const int c = tm.ci(m);
 #pragma unroll
         for (int s = 0; s < 2; ++s) {
-            const float *g = X(4 + s) + c;
             const float h = s ? hB[m] : hA[m];
             float w, Wp, Wm;
             if (h > 0.0f) {
-                w = g[0];
-                Wp = M::sub(g[1], w);
-                Wm = M::sub(w, g[-1]);
+                w = XR(4 + s, c);
+                Wp = M::sub(XR(4 + s, c + 1), w);
+                Wm = M::sub(w, XR(4 + s, c - 1));
             } else {
-                w = g[1];
-                Wp = M::sub(w, g[2]);
-                Wm = M::sub(g[0], w);
+                w = XR(4 + s, c + 1);
+                Wp = M::sub(w, XR(4 + s, c + 2));
+                Wm = M::sub(XR(4 + s, c), w);
             }
             const float dw = M::slope(Wm, Wp);
             const float fl = M::mul(M::add(w, dw), dt);
@@ -238,9 +244,10 @@ __device__ __forceinline__ void advect_tile_team(const AdvectArgs &a, long long 
     if (!ROWS) {
 #pragma unroll
         for (int m = 0; m < CPL; ++m) {
-            if (live && tm.valid(m)) {
+            if (live && tm.valid(m) && MHD_GM(a.b + (base + tm.ci(m)) * 3 + 2, a.b, MHD_NB(f)) &&
+                MHD_GM(a.sA + base + tm.ci(m), a.sA, f.npen * n) && MHD_GM(a.sB + base + tm.ci(m), a.sB, f.npen * n)) {
                 const int c = tm.ci(m);
-                const float sa = X(2)[c - 1], sb = X(3)[c - 1];
+                const float sa = XR(2, c - 1), sb = XR(3, c - 1);
                 a.b[(base + c) * 3 + 1] = M::sub(bA[m], M::sub(flA[m], sa));
                 a.b[(base + c) * 3 + 2] = M::sub(bB[m], M::sub(flB[m], sb));
                 a.sA[base + c] = sa;
@@ -253,7 +260,7 @@ __device__ __forceinline__ void advect_tile_team(const AdvectArgs &a, long long 
         for (int m = 0; m < CPL; ++m) {
             if (!tm.valid(m)) continue;
             const int c = tm.ci(m);
-            const float sa = X(2)[c - 1], sb = X(3)[c - 1];
+            const float sa = XR(2, c - 1), sb = XR(3, c - 1);
             o[m][0] = M::sub(bA[m], M::sub(flA[m], sa));
             o[m][1] = M::sub(bB[m], M::sub(flB[m], sb));
             o[m][2] = sa;
@@ -266,7 +273,8 @@ __device__ __forceinline__ void advect_tile_team(const AdvectArgs &a, long long 
         for (int m = 0; m < CPL; ++m)
             if (live && tm.valid(m))
 #pragma unroll
-                for (int w = 0; w < 4; ++w) OUT[tm.ci(m) * ro + 4 * q + w] = o[m][w];
+                for (int w = 0; w < 4; ++w)
+                    if (MHD_SM(&OUT[tm.ci(m) * ro + 4 * q + w], 4)) OUT[tm.ci(m) * ro + 4 * q + w] = o[m][w];
         __syncthreads();
         const long long kb = (long long)k * f.sk;
         const int p2 = nib(f.pb, 1), p3 = nib(f.pb, 2);
@@ -279,7 +287,9 @@ __device__ __forceinline__ void advect_tile_team(const AdvectArgs &a, long long 
         for (int i = warp; i < n; i += nwarps) {
             if (!on) continue;
             const long long cell = kb + (long long)i * f.si + j0 + qq;
-            dst[cell * dstride] = OUT[i * ro + lane];
+            if (MHD_SM(&OUT[i * ro + lane], 4) && MHD_GM(dst + cell * dstride, w < 2 ? a.b : (w == 2 ? a.sA : a.sB),
+                                                          w < 2 ? MHD_NB(f) : f.npen * n))
+                dst[cell * dstride] = OUT[i * ro + lane];
         }
     }
 }
@@ -311,6 +321,9 @@ __device__ __forceinline__ void advect_b1_cell(const AdvectArgs &a, unsigned c)
     const unsigned cj = (j + 1 == (unsigned)f.ny) ? c - j * sj : c + sj;
     const unsigned ck = (k + 1 == (unsigned)f.nz) ? c - k * sk : c + sk;
     const int p1 = nib(f.pb, 0);
+    const long long ncell = f.npen * f.n;
+    (void)ncell;
+    if (!(MHD_IN(c, ncell) && MHD_IN(cj, ncell) && MHD_IN(ck, ncell))) return;
     float *bp = a.b + (size_t)c * 3 + p1;
     float bx = *bp;
     bx = fsub(bx, a.sA[c]);

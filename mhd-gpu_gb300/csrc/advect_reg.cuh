@@ -17,6 +17,9 @@
 
 #include "fluidx_reg.cuh"
 
+#undef MHD_DBG_FILE
+#define MHD_DBG_FILE 3
+
 namespace mhd {
 
 // shared floats: 8 arrays of ppc runs of n+4 floats (16-byte aligned runs)
@@ -68,6 +71,9 @@ __device__ __forceinline__ void advect_tile_reg(const AdvectArgs &a, long long t
 #pragma unroll
             for (int s = 0; s < CPL; ++s) {
                 const int c = ln.t + s * TPP;
+                if (!(MHD_GM(uo + c * 5 + 1, a.u, MHD_NU(f)) && MHD_GM(uj + c * 5 + 1, a.u, MHD_NU(f)) &&
+                      MHD_GM(uk + c * 5 + 1, a.u, MHD_NU(f)) && MHD_GM(bo + c * 3 + 2, a.b, MHD_NB(f))))
+                    continue;
                 cp_async4(d + kAxRho * PR + c, uo + c * 5);
                 cp_async4(d + kAxM * PR + c, uo + c * 5 + 1);
                 cp_async4(d + kAxRhoJ * PR + c, uj + c * 5);
@@ -87,6 +93,10 @@ __device__ __forceinline__ void advect_tile_reg(const AdvectArgs &a, long long t
         long long gst[2];
         int dst[2];
         bool on[2];
+#if defined(MHD_DEBUG)
+        const float *glo[2];
+        long long gn[2];
+#endif
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
             const int L = lane + 32 * h;
@@ -100,12 +110,17 @@ __device__ __forceinline__ void advect_tile_reg(const AdvectArgs &a, long long t
             const long long cell = (long long)plane * f.sk + jc;
             src[h] = isb ? a.b + cell * 3 + comp : a.u + cell * 5 + comp;
             gst[h] = (isb ? 3 : 5) * f.si;
+#if defined(MHD_DEBUG)
+            glo[h] = isb ? a.b : a.u;
+            gn[h] = isb ? MHD_NB(f) : MHD_NU(f);
+#endif
             dst[h] = on[h] ? arr * PR + qq * R : 0;
         }
         for (int i = warp; i < N; i += nwarps) {
 #pragma unroll
             for (int h = 0; h < 2; ++h)
-                if (on[h]) cp_async4(smem + dst[h] + i, src[h] + (long long)i * gst[h]);
+                if (on[h] && MHD_GM(src[h] + (long long)i * gst[h], glo[h], gn[h]))
+                    cp_async4(smem + dst[h] + i, src[h] + (long long)i * gst[h]);
         }
     }
     cp_async_wait_all();
@@ -203,6 +218,9 @@ __device__ __forceinline__ void advect_tile_reg(const AdvectArgs &a, long long t
 #pragma unroll
             for (int s = 0; s < CPL; ++s) {
                 const int c = ln.t + s * TPP;
+                if (!(MHD_SM(&o[c], 4) && MHD_SM(&o[3 * PR + c], 4) && MHD_GM(gb + c * 3 + 2, a.b, MHD_NB(f)) &&
+                      MHD_GM(ga + c, a.sA, f.npen * f.n) && MHD_GM(gs + c, a.sB, f.npen * f.n)))
+                    continue;
                 gb[c * 3 + p2] = o[c];
                 gb[c * 3 + p3] = o[PR + c];
                 ga[c] = o[2 * PR + c];
@@ -221,7 +239,9 @@ __device__ __forceinline__ void advect_tile_reg(const AdvectArgs &a, long long t
         for (int i = warp; i < N; i += nwarps) {
             if (!on) continue;
             const long long cell = kb + (long long)i * f.si + j0 + qq;
-            dst[cell * dstride] = o[i];
+            if (MHD_SM(&o[i], 4) && MHD_GM(dst + cell * dstride, w < 2 ? a.b : (w == 2 ? a.sA : a.sB),
+                                           w < 2 ? MHD_NB(f) : f.npen * f.n))
+                dst[cell * dstride] = o[i];
         }
     }
 }

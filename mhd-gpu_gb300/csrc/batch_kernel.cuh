@@ -34,6 +34,9 @@
 #include "cfl_kernel.cuh"
 #include "fluidx_kernel.cuh"
 
+#undef MHD_DBG_FILE
+#define MHD_DBG_FILE 5
+
 namespace mhd {
 
 constexpr int kBatchMaxPencil = MHD_BATCH_MAX_PENCIL;
@@ -178,7 +181,7 @@ batch_class_kernel(const __grid_constant__ ClassWork w)
     __shared__ unsigned s_start[3 * kGroupBoxes + 1];
     __shared__ int s_group[3 * kGroupBoxes];
     __shared__ unsigned char s_ok[3 * kGroupBoxes];
-    const int ne = 3 * w.nb;
+    const int ne = MHD_IN(w.nb, kGroupBoxes + 1) ? 3 * w.nb : 0;
     for (int x = threadIdx.x; x <= ne; x += blockDim.x) s_start[x] = (unsigned)w.start[x];
     for (int x = threadIdx.x; x < ne; x += blockDim.x) {
         s_group[x] = w.group[x];
@@ -196,7 +199,7 @@ batch_class_kernel(const __grid_constant__ ClassWork w)
             int e = -1, run = 0;
             long long local = 0;
             if (it < total) {
-                while (s_start[ecur + 1] <= it) ++ecur;   // last entry with start <= it
+                while (MHD_IN(ecur + 1, ne + 1) && s_start[ecur + 1] <= it) ++ecur;   // last entry with start <= it
                 e = ecur;
                 local = (long long)(it - s_start[e]);
                 run = 1;

@@ -6,12 +6,16 @@
 
 #include "kernels.cuh"
 
+#undef MHD_DBG_FILE
+#define MHD_DBG_FILE 7
+
 namespace mhd {
 
 __device__ __forceinline__ float cfl_cell_speed(const float *__restrict__ u, const float *__restrict__ b,
                                                 int nx, int ny, int nz, int mode, long long c)
 {
     float uu[5], bb[3];
+    if (!MHD_IN(c, (long long)nx * ny * nz)) return 0.0f;
 #pragma unroll
     for (int ii = 0; ii < 5; ++ii) uu[ii] = __ldg(u + c * 5 + ii);
     if (mode == MHD_CFL_C) {
@@ -28,6 +32,9 @@ __device__ __forceinline__ float cfl_cell_speed(const float *__restrict__ u, con
     const long long cx = ((long long)k * ny + j) * nx + ip;
     const long long cy = ((long long)k * ny + jp) * nx + i;
     const long long cz = ((long long)kp * ny + j) * nx + i;
+    const long long ncell = (long long)nx * ny * nz;
+    (void)ncell;
+    if (!(MHD_IN(cx, ncell) && MHD_IN(cy, ncell) && MHD_IN(cz, ncell))) return 0.0f;
     bb[0] = fdiv(fadd(__ldg(b + c * 3 + 0), __ldg(b + cx * 3 + 0)), 2.0f);
     bb[1] = fdiv(fadd(__ldg(b + c * 3 + 1), __ldg(b + cy * 3 + 1)), 2.0f);
     bb[2] = fdiv(fadd(__ldg(b + c * 3 + 2), __ldg(b + cz * 3 + 2)), 2.0f);
@@ -62,7 +69,7 @@ __device__ __forceinline__ void clock_tick(mhdgpu_clock *clk, double cfl_number,
     const float d = dt_rule(inv, cfl_number, clk->t, tf);
     clk->dt = d;
     clk->t = fadd(clk->t, 2.0f * d);
-    if (dt_log) dt_log[clk->iter] = d;
+    if (dt_log && MHD_IN(clk->iter, 1 << 30)) dt_log[clk->iter] = d;
     clk->iter += 1;
 }
 

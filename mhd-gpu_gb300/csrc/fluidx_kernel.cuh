@@ -33,6 +33,9 @@
 #include "fluidx_reg.cuh"
 #include "kernels.cuh"
 
+#undef MHD_DBG_FILE
+#define MHD_DBG_FILE 2
+
 namespace mhd {
 
 // shared-memory geometry (floats), shared by the kernel and its launcher
@@ -109,13 +112,20 @@ __device__ __forceinline__ void fluidx_tile_team(const FluidxArgs &a, long long 
     const int rs = tm.rs();
     float *x = XA + (size_t)q * fx_xpen(n) + 1;
     auto X = [&](int r) { return x + r * rs; };
+    // value of exchange row r at cell i (-1 <= i <= n+1), of the staged u
+    auto XR = [&](int r, int i) { return (MHD_IN(i + 1, rs) && MHD_SM(X(r) + i, 4)) ? X(r)[i] : 0.0f; };
+    auto UR = [&](int i) { return MHD_SM(us + i, 4) ? us[i] : 0.0f; };
+    (void)UR;
 
     // ---- stage u (kept) and b (transient) ----
     float bc[CPL][3];
     const float *bjp = nullptr, *bkp = nullptr;   // !ROWS: b of the j+1 and k+1 pencils
     if (!ROWS) {
-        block_copy_in(US, a.u_in + p0 * 5 * n, (long long)nvalid * 5 * n, threadIdx.x, blockDim.x);
-        block_copy_in(XA, a.b + p0 * 3 * n, (long long)nvalid * 3 * n, threadIdx.x, blockDim.x);
+        if (MHD_GM(a.u_in + p0 * 5 * n, a.u_in, MHD_NU(f)) &&
+            MHD_GM(a.u_in + (p0 + nvalid) * 5 * n - 1, a.u_in, MHD_NU(f)))
+            block_copy_in(US, a.u_in + p0 * 5 * n, (long long)nvalid * 5 * n, threadIdx.x, blockDim.x);
+        if (MHD_GM(a.b + p0 * 3 * n, a.b, MHD_NB(f)) && MHD_GM(a.b + (p0 + nvalid) * 3 * n - 1, a.b, MHD_NB(f)))
+            block_copy_in(XA, a.b + p0 * 3 * n, (long long)nvalid * 3 * n, threadIdx.x, blockDim.x);
         __syncthreads();
         // b3x = b/2 ; b3x(1) += cshift(b3x(1),1) ; b3x(2) += b(2,jp)/2 ;
         // b3x(3) += b(3,kp)/2   (fluidx.c:71-81; the halvings are exact).
@@ -130,7 +140,8 @@ __device__ __forceinline__ void fluidx_tile_team(const FluidxArgs &a, long long 
         for (int m = 0; m < CPL; ++m) {
             const int c = tm.ci(m);
             const int cp = (c + 1 == n) ? 0 : c + 1;
-            if (live && tm.valid(m)) {
+            if (live && tm.valid(m) && MHD_SM(pb + c * 3, 12) && MHD_SM(pb + cp * 3, 4) &&
+                MHD_GM(bjp + c * 3 + 1, a.b, MHD_NB(f)) && MHD_GM(bkp + c * 3 + 2, a.b, MHD_NB(f))) {
                 bc[m][0] = fadd(0.5f * pb[c * 3 + 0], 0.5f * pb[cp * 3 + 0]);
                 bc[m][1] = fadd(0.5f * pb[c * 3 + 1], 0.5f * bjp[c * 3 + 1]);
                 bc[m][2] = fadd(0.5f * pb[c * 3 + 2], 0.5f * bkp[c * 3 + 2]);
@@ -173,11 +184,12 @@ __device__ __forceinline__ void fluidx_tile_team(const FluidxArgs &a, long long 
             const float *gb = a.b + rowc * 3;
 #pragma unroll
             for (int h = 0; h < 2; ++h) {
-                if (us_on[h]) cp_async4(&US[us_off[h] + i * 5], gu + lane + 32 * h);
-                if (sb_on[h]) cp_async4(&SB[sb_off[h] + i * 3], gb + gb_off[h]);
+                if (us_on[h] && MHD_GM(gu + lane + 32 * h, a.u_in, MHD_NU(f)))
+                    cp_async4(&US[us_off[h] + i * 5], gu + lane + 32 * h);
+                if (sb_on[h] && MHD_GM(gb + gb_off[h], a.b, MHD_NB(f))) cp_async4(&SB[sb_off[h] + i * 3], gb + gb_off[h]);
             }
-            if (sk_on)
-                cp_async4(&SK[i * ks + lane], a.b + (kpb + (long long)i * f.si + j0 + lane) * 3 + pb2);
+            const float *gk = a.b + (kpb + (long long)i * f.si + j0 + lane) * 3 + pb2;
+            if (sk_on && MHD_GM(gk, a.b, MHD_NB(f))) cp_async4(&SK[i * ks + lane], gk);
         }
         cp_async_wait_all();
         __syncthreads();
@@ -186,7 +198,8 @@ __device__ __forceinline__ void fluidx_tile_team(const FluidxArgs &a, long long 
         for (int m = 0; m < CPL; ++m) {
             const int c = tm.ci(m);
             const int cp = (c + 1 == n) ? 0 : c + 1;
-            if (live && tm.valid(m)) {
+            if (live && tm.valid(m) && MHD_SM(sb0 + c * 3, 12) && MHD_SM(sb0 + cp * 3, 4) &&
+                MHD_SM(sb1 + c * 3 + 1, 4) && MHD_SM(&SK[c * ks + q], 4)) {
                 bc[m][0] = fadd(0.5f * sb0[c * 3 + 0], 0.5f * sb0[cp * 3 + 0]);
                 bc[m][1] = fadd(0.5f * sb0[c * 3 + 1], 0.5f * sb1[c * 3 + 1]);
                 bc[m][2] = fadd(0.5f * sb0[c * 3 + 2], 0.5f * SK[c * ks + q]);
@@ -212,7 +225,7 @@ __device__ __forceinline__ void fluidx_tile_team(const FluidxArgs &a, long long 
             float uu[5];
             if (live) {
 #pragma unroll
-                for (int ii = 0; ii < 5; ++ii) uu[ii] = us[tm.ci(m) * 5 + ii];
+                for (int ii = 0; ii < 5; ++ii) uu[ii] = UR(tm.ci(m) * 5 + ii);
             } else {
                 uu[0] = 1.0f; uu[1] = 0.0f; uu[2] = 0.0f; uu[3] = 0.0f; uu[4] = 1.0f;
             }
@@ -230,7 +243,7 @@ __device__ __forceinline__ void fluidx_tile_team(const FluidxArgs &a, long long 
         for (int m = 0; m < CPL; ++m)
 #pragma unroll
             for (int ii = 0; ii < 5; ++ii) if (tm.valid(m)) {
-                const float uu = us[tm.ci(m) * 5 + ii];
+                const float uu = UR(tm.ci(m) * 5 + ii);
                 const float vv = M::divy(v[m][ii], cd, yc);
                 u1[m][ii] = M::mul(c, M::add(uu, vv));
                 tm.put(X(ii), m, M::sub(uu, vv));
@@ -241,7 +254,7 @@ __device__ __forceinline__ void fluidx_tile_team(const FluidxArgs &a, long long 
         for (int m = 0; m < CPL; ++m)
 #pragma unroll
             for (int ii = 0; ii < 5; ++ii) if (tm.valid(m)) {
-                const float fl = M::mul(c, X(ii)[tm.ci(m) + 1]);
+                const float fl = M::mul(c, XR(ii, tm.ci(m) + 1));
                 u1[m][ii] = 0.5f * M::sub(u1[m][ii], fl);
                 tm.put(X(5 + ii), m, u1[m][ii]);
             }
@@ -251,8 +264,8 @@ __device__ __forceinline__ void fluidx_tile_team(const FluidxArgs &a, long long 
         for (int m = 0; m < CPL; ++m)
 #pragma unroll
             for (int ii = 0; ii < 5; ++ii) if (tm.valid(m)) {
-                const float d = M::sub(u1[m][ii], X(5 + ii)[tm.ci(m) - 1]);
-                u1[m][ii] = M::add(us[tm.ci(m) * 5 + ii], M::mul(-hdt, d));
+                const float d = M::sub(u1[m][ii], XR(5 + ii, tm.ci(m) - 1));
+                u1[m][ii] = M::add(UR(tm.ci(m) * 5 + ii), M::mul(-hdt, d));
             }
     }
     tm.sync();   // every read of rows 5-9 is done before they are rewritten
@@ -297,12 +310,12 @@ __device__ __forceinline__ void fluidx_tile_team(const FluidxArgs &a, long long 
         for (int m = 0; m < CPL; ++m)
 #pragma unroll
             for (int ii = 0; ii < 5; ++ii) if (tm.valid(m)) {
-                const float *fr = X(ii) + tm.ci(m), *wl = X(5 + ii) + tm.ci(m);
-                const float f0 = fr[0];
-                const float dfr = M::slope(M::sub(fr[1], f0), M::sub(f0, fr[-1]));
-                const float fl0 = M::mul(c, wl[1]);
-                const float flp = M::mul(c, wl[2]);
-                const float flm = M::mul(c, wl[0]);
+                const int cm = tm.ci(m);
+                const float f0 = XR(ii, cm);
+                const float dfr = M::slope(M::sub(XR(ii, cm + 1), f0), M::sub(f0, XR(ii, cm - 1)));
+                const float fl0 = M::mul(c, XR(5 + ii, cm + 1));
+                const float flp = M::mul(c, XR(5 + ii, cm + 2));
+                const float flm = M::mul(c, XR(5 + ii, cm));
                 const float dfl = M::slope(M::sub(fl0, flp), M::sub(flm, fl0));
                 fx[m][ii] = 0.5f * M::add(M::sub(f0, fl0), M::sub(dfr, dfl));
             }
@@ -325,9 +338,9 @@ __device__ __forceinline__ void fluidx_tile_team(const FluidxArgs &a, long long 
             float uf[5];
 #pragma unroll
             for (int ii = 0; ii < 5; ++ii) {
-                const float d = M::sub(fx[m][ii], X(ii)[cc - 1]);
-                const float un = M::add(us[cc * 5 + ii], M::mul(mdt, d));
-                us[cc * 5 + ii] = un;
+                const float d = M::sub(fx[m][ii], XR(ii, cc - 1));
+                const float un = M::add(UR(cc * 5 + ii), M::mul(mdt, d));
+                if (MHD_SM(us + cc * 5 + ii, 4)) us[cc * 5 + ii] = un;
                 uf[ii] = un;
                 s += un;
                 if (ii == 0) r = un;
@@ -337,6 +350,11 @@ __device__ __forceinline__ void fluidx_tile_team(const FluidxArgs &a, long long 
             if (fold_cfl) {
                 // the CFL fast speed of the updated cell, as cfl_cell_speed forms it
                 float bb[3];
+                if (!(MHD_GM(bown + cc * 3, a.b, MHD_NB(f)) && MHD_GM(bown + cc * 3 + 2, a.b, MHD_NB(f)) &&
+                      MHD_GM(bown + ((cc + 1 == n) ? 0 : cc + 1) * 3, a.b, MHD_NB(f)) &&
+                      MHD_GM(bjp + cc * 3 + 1, a.b, MHD_NB(f)) &&
+                      MHD_GM(bkp + cc * 3 + 2, a.b, MHD_NB(f))))
+                    continue;
                 if (a.cfl_mode == MHD_CFL_C) {
                     bb[0] = bown[cc * 3 + 0];
                     bb[1] = bown[cc * 3 + 1];
@@ -358,7 +376,9 @@ __device__ __forceinline__ void fluidx_tile_team(const FluidxArgs &a, long long 
     if (bad) flag_health(a.health, bad);
     __syncthreads();
     if (!ROWS) {
-        block_copy_out(a.u_out + p0 * 5 * n, US, (long long)nvalid * 5 * n, threadIdx.x, blockDim.x);
+        if (MHD_GM(a.u_out + p0 * 5 * n, a.u_out, MHD_NU(f)) &&
+            MHD_GM(a.u_out + (p0 + nvalid) * 5 * n - 1, a.u_out, MHD_NU(f)))
+            block_copy_out(a.u_out + p0 * 5 * n, US, (long long)nvalid * 5 * n, threadIdx.x, blockDim.x);
     } else {
         const long long kb = (long long)k * f.sk;
         const int ru = 5 * nvalid;
@@ -375,7 +395,8 @@ __device__ __forceinline__ void fluidx_tile_team(const FluidxArgs &a, long long 
             float *g = a.u_out + (kb + (long long)i * f.si + j0) * 5;
 #pragma unroll
             for (int h = 0; h < 2; ++h)
-                if (on[h]) g[lane + 32 * h] = US[off[h] + i * 5];
+                if (on[h] && MHD_SM(&US[off[h] + i * 5], 4) && MHD_GM(g + lane + 32 * h, a.u_out, MHD_NU(f)))
+                    g[lane + 32 * h] = US[off[h] + i * 5];
         }
     }
 }

@@ -22,7 +22,15 @@
 #include "kernels.cuh"
 #include "tma_rows.cuh"
 
+#undef MHD_DBG_FILE
+#define MHD_DBG_FILE 1
+
 namespace mhd {
+
+// floats of u and of b of a frame's box (the extents the debug build checks
+// global indices against)
+#define MHD_NU(f) (5LL * (f).npen * (f).n)
+#define MHD_NB(f) (3LL * (f).npen * (f).n)
 
 // shared-memory geometry (floats); every offset is a multiple of 4 floats
 __host__ __device__ inline int fxr_cs(int n) { return n + 4; }                    // a component of u
@@ -60,6 +68,11 @@ struct Lanes {
 template <int K>
 __device__ __forceinline__ void lds_run(const float *p, float (&v)[K])
 {
+    if (!MHD_SM(p, 4 * K)) {
+#pragma unroll
+        for (int i = 0; i < K; ++i) v[i] = 0.0f;
+        return;
+    }
     if constexpr (K % 4 == 0) {
 #pragma unroll
         for (int i = 0; i < K / 4; ++i) {
@@ -81,6 +94,7 @@ __device__ __forceinline__ void lds_run(const float *p, float (&v)[K])
 template <int K>
 __device__ __forceinline__ void sts_run(float *p, const float (&v)[K])
 {
+    if (!MHD_SM(p, 4 * K)) return;
     if constexpr (K % 4 == 0) {
 #pragma unroll
         for (int i = 0; i < K / 4; ++i)
@@ -135,7 +149,8 @@ __device__ __forceinline__ void rows_vec_put_u(float *d, const float4 (&v)[5], c
     const float e[20] = {v[0].x, v[0].y, v[0].z, v[0].w, v[1].x, v[1].y, v[1].z, v[1].w, v[2].x, v[2].y,
                          v[2].z, v[2].w, v[3].x, v[3].y, v[3].z, v[3].w, v[4].x, v[4].y, v[4].z, v[4].w};
 #pragma unroll
-    for (int x = 0; x < 20; ++x) d[(x / 5) * PS + co[x % 5]] = e[x];
+    for (int x = 0; x < 20; ++x)
+        if (MHD_SM(&d[(x / 5) * PS + co[x % 5]], 4)) d[(x / 5) * PS + co[x % 5]] = e[x];
 }
 
 template <int N>
@@ -156,26 +171,28 @@ __device__ __forceinline__ void rows_vec_stage(const Frame &f, const float *u_in
     for (int un = threadIdx.x; un < units; un += blockDim.x) {
         const int Q = un / N, i = un - Q * N;
         const long long cell = kb + (long long)i * f.si + j0 + 4 * Q;
-        {
+        if (MHD_GM(u_in + cell * 5, u_in, MHD_NU(f)) && MHD_GM(u_in + cell * 5 + 19, u_in, MHD_NU(f))) {
             const float4 *g = reinterpret_cast<const float4 *>(u_in + cell * 5);
             float4 v[5];
 #pragma unroll
             for (int w = 0; w < 5; ++w) v[w] = g[w];
             rows_vec_put_u<PS>(US + 4 * Q * PS + i, v, co);
         }
-        {
+        if (MHD_GM(b + cell * 3, b, MHD_NB(f)) && MHD_GM(b + cell * 3 + 11, b, MHD_NB(f))) {
             const float4 *g = reinterpret_cast<const float4 *>(b + cell * 3);
             const float4 v0 = g[0], v1 = g[1], v2 = g[2];
             const float e[12] = {v0.x, v0.y, v0.z, v0.w, v1.x, v1.y, v1.z, v1.w, v2.x, v2.y, v2.z, v2.w};
             float *d = SB + 4 * Q * BSR + 3 * i;
 #pragma unroll
-            for (int x = 0; x < 12; ++x) d[(x / 3) * BSR + cb[x % 3]] = e[x];
+            for (int x = 0; x < 12; ++x)
+                if (MHD_SM(&d[(x / 3) * BSR + cb[x % 3]], 4)) d[(x / 3) * BSR + cb[x % 3]] = e[x];
         }
         {
             const float *g = b + (kpb + (long long)i * f.si + j0 + 4 * Q) * 3 + pb2;
             float *d = SK + 4 * Q * KS + i;
 #pragma unroll
-            for (int x = 0; x < 4; ++x) d[x * KS] = g[3 * x];
+            for (int x = 0; x < 4; ++x)
+                if (MHD_SM(&d[x * KS], 4) && MHD_GM(g + 3 * x, b, MHD_NB(f))) d[x * KS] = g[3 * x];
         }
     }
     // b of the column after the tile (column 0 when the tile ends the frame),
@@ -184,7 +201,8 @@ __device__ __forceinline__ void rows_vec_stage(const Frame &f, const float *u_in
     if (jx >= f.ny) jx -= f.ny;
     for (int h = threadIdx.x; h < 3 * N; h += blockDim.x) {
         const int s = h / N, i = h - s * N;
-        SB[ppc * BSR + 3 * i + cb[s]] = b[(kb + (long long)i * f.si + jx) * 3 + s];
+        const float *g = b + (kb + (long long)i * f.si + jx) * 3 + s;
+        if (MHD_SM(&SB[ppc * BSR + 3 * i + cb[s]], 4) && MHD_GM(g, b, MHD_NB(f))) SB[ppc * BSR + 3 * i + cb[s]] = *g;
     }
 }
 
@@ -205,8 +223,11 @@ __device__ __forceinline__ void rows_vec_writeback(const Frame &f, float *u_out,
         const float *d = US + 4 * Q * PS + i;
         float e[20];
 #pragma unroll
-        for (int x = 0; x < 20; ++x) e[x] = d[(x / 5) * PS + co[x % 5]];
-        float4 *g = reinterpret_cast<float4 *>(u_out + (kb + (long long)i * f.si + j0 + 4 * Q) * 5);
+        for (int x = 0; x < 20; ++x)
+            e[x] = MHD_SM(&d[(x / 5) * PS + co[x % 5]], 4) ? d[(x / 5) * PS + co[x % 5]] : 0.0f;
+        float *go = u_out + (kb + (long long)i * f.si + j0 + 4 * Q) * 5;
+        if (!(MHD_GM(go, u_out, MHD_NU(f)) && MHD_GM(go + 19, u_out, MHD_NU(f)))) continue;
+        float4 *g = reinterpret_cast<float4 *>(go);
 #pragma unroll
         for (int w = 0; w < 5; ++w) g[w] = make_float4(e[4 * w], e[4 * w + 1], e[4 * w + 2], e[4 * w + 3]);
     }
@@ -266,10 +287,13 @@ __device__ __forceinline__ void fluidx_tile_reg(const FluidxArgs &a, long long t
                 float *d = US + qq * PS + cc;
                 const float *s = gu + (long long)c * 5;
 #pragma unroll
-                for (int ii = 0; ii < 5; ++ii) cp_async4(d + ii * CS, s + ii);
+                for (int ii = 0; ii < 5; ++ii)
+                    if (MHD_GM(s + ii, a.u_in, MHD_NU(f))) cp_async4(d + ii * CS, s + ii);
             }
             // b as it lies; completes this thread's u copies too
-            block_copy_in(BS, a.b + p0 * 3 * N, (long long)nvalid * 3 * N, threadIdx.x, blockDim.x);
+            if (MHD_GM(a.b + p0 * 3 * N, a.b, MHD_NB(f)) &&
+                MHD_GM(a.b + (p0 + nvalid) * 3 * N - 1, a.b, MHD_NB(f)))
+                block_copy_in(BS, a.b + p0 * 3 * N, (long long)nvalid * 3 * N, threadIdx.x, blockDim.x);
             __syncthreads();
             const int jp = (jq + 1 == f.ny) ? 0 : jq + 1;
             const int kp = (kq + 1 == f.nz) ? 0 : kq + 1;
@@ -279,8 +303,8 @@ __device__ __forceinline__ void fluidx_tile_reg(const FluidxArgs &a, long long t
                 lds_run<3 * CPL>(BS + q * BSC + c0 * 3, bo);
 #pragma unroll
                 for (int m = 0; m < CPL; ++m) {
-                    bj[m] = bjp[(c0 + m) * 3 + 1];
-                    bk[m] = bkp[(c0 + m) * 3 + 2];
+                    bj[m] = MHD_GM(bjp + (c0 + m) * 3 + 1, a.b, MHD_NB(f)) ? bjp[(c0 + m) * 3 + 1] : 0.0f;
+                    bk[m] = MHD_GM(bkp + (c0 + m) * 3 + 2, a.b, MHD_NB(f)) ? bkp[(c0 + m) * 3 + 2] : 0.0f;
                 }
             }
         } else {
@@ -340,11 +364,11 @@ __device__ __forceinline__ void fluidx_tile_reg(const FluidxArgs &a, long long t
                     const float *gk = a.b + (kpb + (long long)i0 * f.si) * 3;
 #pragma unroll
                     for (int s = 0; s < 5; ++s)
-                        if (uon[s]) cp_async4(&US[uso[s] + i0], gu + ugo[s]);
+                        if (uon[s] && MHD_GM(gu + ugo[s], a.u_in, MHD_NU(f))) cp_async4(&US[uso[s] + i0], gu + ugo[s]);
 #pragma unroll
                     for (int s = 0; s < 4; ++s)
-                        if (bon[s]) cp_async4(&SB[bso[s] + 3 * i0], gb + bgo[s]);
-                    if (kon) cp_async4(&SK[kso + i0], gk + kgo);
+                        if (bon[s] && MHD_GM(gb + bgo[s], a.b, MHD_NB(f))) cp_async4(&SB[bso[s] + 3 * i0], gb + bgo[s]);
+                    if (kon && MHD_GM(gk + kgo, a.b, MHD_NB(f))) cp_async4(&SK[kso + i0], gk + kgo);
                 }
             } else {
                 const int ru = 5 * nvalid, rb = 3 * (nvalid + 1);
@@ -373,11 +397,13 @@ __device__ __forceinline__ void fluidx_tile_reg(const FluidxArgs &a, long long t
                     const float *gb = a.b + rowc * 3;
 #pragma unroll
                     for (int h = 0; h < 2; ++h) {
-                        if (us_on[h]) cp_async4(&US[us_off[h] + i], gu + lane + 32 * h);
-                        if (sb_on[h]) cp_async4(&SB[sb_off[h] + i * 3], gb + gb_off[h]);
+                        if (us_on[h] && MHD_GM(gu + lane + 32 * h, a.u_in, MHD_NU(f)))
+                            cp_async4(&US[us_off[h] + i], gu + lane + 32 * h);
+                        if (sb_on[h] && MHD_GM(gb + gb_off[h], a.b, MHD_NB(f)))
+                            cp_async4(&SB[sb_off[h] + i * 3], gb + gb_off[h]);
                     }
-                    if (sk_on)
-                        cp_async4(&SK[lane * KS + i], a.b + (kpb + (long long)i * f.si + j0 + lane) * 3 + pb2);
+                    const float *gk = a.b + (kpb + (long long)i * f.si + j0 + lane) * 3 + pb2;
+                    if (sk_on && MHD_GM(gk, a.b, MHD_NB(f))) cp_async4(&SK[lane * KS + i], gk);
                 }
             }
             cp_async_wait_all();
@@ -535,20 +561,24 @@ __device__ __forceinline__ void fluidx_tile_reg(const FluidxArgs &a, long long t
         // as cfl_cell_speed forms it
         if (!ROWS && a.cfl != nullptr) {
             const float *bs = BS + q * BSC + c0 * 3;   // this run's staged b
-            const float nb0 = ln.from(live ? bs[0] : 0.0f, 1);
+            const float nb0 = ln.from(live && MHD_SM(bs, 4) ? bs[0] : 0.0f, 1);
             float cfl_c = 0.0f;
             if (live) {
 #pragma unroll
                 for (int m = 0; m < CPL; ++m) {
                     float um[5], bb[3];
 #pragma unroll
-                    for (int ii = 0; ii < 5; ++ii) um[ii] = us[ii * CS + m];
+                    for (int ii = 0; ii < 5; ++ii) um[ii] = MHD_SM(&us[ii * CS + m], 4) ? us[ii * CS + m] : 1.0f;
+                    if (!MHD_SM(bs + 3 * m, 12) || !MHD_SM(bs + 3 * (m + 1 < CPL ? m + 1 : m), 4)) continue;
                     if (a.cfl_mode == MHD_CFL_C) {
                         bb[0] = bs[3 * m]; bb[1] = bs[3 * m + 1]; bb[2] = bs[3 * m + 2];
                         cfl_c = fmaxf(cfl_c, cfl_speed_c(um, bb));
                     } else {
                         const float bnext = (m + 1 < CPL) ? bs[3 * (m + 1)] : nb0;
                         bb[0] = fdiv(fadd(bs[3 * m], bnext), 2.0f);
+                        if (!MHD_GM(bjp + (c0 + m) * 3 + 1, a.b, MHD_NB(f)) ||
+                            !MHD_GM(bkp + (c0 + m) * 3 + 2, a.b, MHD_NB(f)))
+                            continue;
                         bb[1] = fdiv(fadd(bs[3 * m + 1], bjp[(c0 + m) * 3 + 1]), 2.0f);
                         bb[2] = fdiv(fadd(bs[3 * m + 2], bkp[(c0 + m) * 3 + 2]), 2.0f);
                         cfl_c = fmaxf(cfl_c, cfl_speed_averaged(um, bb));
@@ -575,8 +605,12 @@ __device__ __forceinline__ void fluidx_tile_reg(const FluidxArgs &a, long long t
                 const float *src = US + qq * PS + cc;
                 float4 c[5];
 #pragma unroll
-                for (int ii = 0; ii < 5; ++ii) c[ii] = *reinterpret_cast<const float4 *>(src + ii * CS);
-                float4 *dst = reinterpret_cast<float4 *>(g + (size_t)(qq * N + cc) * 5);
+                for (int ii = 0; ii < 5; ++ii)
+                    c[ii] = MHD_SM(src + ii * CS, 16) ? *reinterpret_cast<const float4 *>(src + ii * CS)
+                                                      : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                float *go = g + (size_t)(qq * N + cc) * 5;
+                if (!(MHD_GM(go, a.u_out, MHD_NU(f)) && MHD_GM(go + 19, a.u_out, MHD_NU(f)))) continue;
+                float4 *dst = reinterpret_cast<float4 *>(go);
                 dst[0] = make_float4(c[0].x, c[1].x, c[2].x, c[3].x);
                 dst[1] = make_float4(c[4].x, c[0].y, c[1].y, c[2].y);
                 dst[2] = make_float4(c[3].y, c[4].y, c[0].z, c[1].z);
@@ -587,7 +621,8 @@ __device__ __forceinline__ void fluidx_tile_reg(const FluidxArgs &a, long long t
             const int nf = nvalid * 5 * N;
             for (int e = threadIdx.x; e < nf; e += blockDim.x) {
                 const int cell = e / 5, comp = e - 5 * cell, qq = cell / N, cc = cell - qq * N;
-                g[e] = US[qq * PS + comp * CS + cc];
+                if (MHD_SM(&US[qq * PS + comp * CS + cc], 4) && MHD_GM(g + e, a.u_out, MHD_NU(f)))
+                    g[e] = US[qq * PS + comp * CS + cc];
             }
         }
     } else {
@@ -617,7 +652,8 @@ __device__ __forceinline__ void fluidx_tile_reg(const FluidxArgs &a, long long t
                 float *g = a.u_out + (kb + (long long)i0 * f.si) * 5;
 #pragma unroll
                 for (int s = 0; s < 5; ++s)
-                    if (on[s]) g[go[s]] = US[so[s] + i0];
+                    if (on[s] && MHD_SM(&US[so[s] + i0], 4) && MHD_GM(g + go[s], a.u_out, MHD_NU(f)))
+                        g[go[s]] = US[so[s] + i0];
             }
         } else {
             const long long kb = (long long)k * f.sk;
@@ -635,7 +671,8 @@ __device__ __forceinline__ void fluidx_tile_reg(const FluidxArgs &a, long long t
                 float *g = a.u_out + (kb + (long long)i * f.si + j0) * 5;
 #pragma unroll
                 for (int h = 0; h < 2; ++h)
-                    if (on[h]) g[lane + 32 * h] = US[off[h] + i];
+                    if (on[h] && MHD_SM(&US[off[h] + i], 4) && MHD_GM(g + lane + 32 * h, a.u_out, MHD_NU(f)))
+                        g[lane + 32 * h] = US[off[h] + i];
             }
         }
     }

@@ -7,8 +7,12 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "mhd_debug.cuh"
 #include "mhd_math.cuh"
 #include "mhdgpu.h"   // include/ is on the include path (build.py)
+
+#undef MHD_DBG_FILE
+#define MHD_DBG_FILE 9
 
 namespace mhd {
 
@@ -145,15 +149,16 @@ struct Team {
         if (!valid(m)) return;
         const int c = m * TPP + t;
         const int nn = len();
-        row[c] = v;
+        // a row holds cells -1 .. n+1 (the halo cells -1, n, n+1 included)
+        if (MHD_SM(&row[c], 4) && MHD_IN(c, nn)) row[c] = v;
         if (FULL) {
-            if (m == CPL - 1 && t == TPP - 1) row[-1] = v;
-            if (m == 0 && t == 0) row[nn] = v;
-            if (m == 0 && t == 1) row[nn + 1] = v;
+            if (m == CPL - 1 && t == TPP - 1 && MHD_SM(&row[-1], 4)) row[-1] = v;
+            if (m == 0 && t == 0 && MHD_SM(&row[nn], 4)) row[nn] = v;
+            if (m == 0 && t == 1 && MHD_SM(&row[nn + 1], 4)) row[nn + 1] = v;
         } else {
-            if (c == nn - 1) row[-1] = v;
-            if (c == 0) row[nn] = v;
-            if (c == (nn > 1 ? 1 : 0)) row[nn + 1] = v;
+            if (c == nn - 1 && MHD_SM(&row[-1], 4)) row[-1] = v;
+            if (c == 0 && MHD_SM(&row[nn], 4)) row[nn] = v;
+            if (c == (nn > 1 ? 1 : 0) && MHD_SM(&row[nn + 1], 4)) row[nn + 1] = v;
         }
     }
 
@@ -173,11 +178,11 @@ struct Team {
         for (int o = (TPP < 32 ? TPP : 32) / 2; o > 0; o >>= 1) x = fmaxf(x, __shfl_xor_sync(0xffffffffu, x, o));
         if (WPP <= 1) return x;
         const int w = t >> 5;
-        if ((t & 31) == 0) red[w] = x;
+        if ((t & 31) == 0 && MHD_SM(&red[w], 4)) red[w] = x;
         __syncthreads();
-        float r = red[0];
+        float r = MHD_SM(red, 4 * WPP) ? red[0] : 0.0f;
 #pragma unroll
-        for (int i = 1; i < WPP; ++i) r = fmaxf(r, red[i]);
+        for (int i = 1; i < WPP; ++i) r = fmaxf(r, MHD_SM(red, 4 * WPP) ? red[i] : 0.0f);
         __syncthreads();
         return r;
     }
@@ -226,12 +231,14 @@ __device__ __forceinline__ void flag_health(unsigned *health, unsigned bits)
 // destination before its wait.
 __device__ __forceinline__ void cp_async4(float *smem_dst, const float *gmem_src)
 {
+    if (!MHD_SM(smem_dst, 4)) return;
     const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem_dst));
     asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem_src));
 }
 
 __device__ __forceinline__ void cp_async16(void *smem_dst, const void *gmem_src)
 {
+    if (!MHD_SM(smem_dst, 16)) return;
     const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem_dst));
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem_src));
 }
@@ -268,9 +275,11 @@ __device__ __forceinline__ void block_copy_out(float *__restrict__ dst, const fl
         const float4 *s4 = reinterpret_cast<const float4 *>(src);
         float4 *d4 = reinterpret_cast<float4 *>(dst);
         const long long n4 = count >> 2;
-        for (long long i = tid; i < n4; i += nthreads) d4[i] = s4[i];
+        for (long long i = tid; i < n4; i += nthreads)
+            if (MHD_SM(s4 + i, 16)) d4[i] = s4[i];
     } else {
-        for (long long i = tid; i < count; i += nthreads) dst[i] = src[i];
+        for (long long i = tid; i < count; i += nthreads)
+            if (MHD_SM(src + i, 4)) dst[i] = src[i];
     }
 }
 

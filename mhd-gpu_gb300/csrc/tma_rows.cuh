@@ -12,6 +12,9 @@
 #include "kernels.cuh"
 #include "tma.cuh"
 
+#undef MHD_DBG_FILE
+#define MHD_DBG_FILE 8
+
 namespace mhd {
 
 // pencils per tile of the TMA-staged fluid tile (the maps' box width)
@@ -79,12 +82,14 @@ __device__ __forceinline__ bool tma_rows_stage(const Frame &f, const RowMaps &mp
         for (int pr = warp; pr < NB * (WU / 4); pr += nwarps) {
             const int w = pr % (WU / 4), i = (pr / (WU / 4)) * 32 + lane;
             if (i >= N) continue;
+            if (!MHD_SM(&R4[i * (WU / 4) + w], 16)) continue;
             const float4 v = R4[i * (WU / 4) + w];
             const float e4[4] = {v.x, v.y, v.z, v.w};
 #pragma unroll
             for (int e = 0; e < 4; ++e) {
                 const int idx = 4 * w + e, qq = idx / 5, s = idx - 5 * qq;
-                if (qq < nvalid) US[qq * PS + nib(f.iu, s) * CS + i] = e4[e];
+                if (qq < nvalid && MHD_SM(&US[qq * PS + nib(f.iu, s) * CS + i], 4))
+                    US[qq * PS + nib(f.iu, s) * CS + i] = e4[e];
             }
         }
     }
@@ -95,8 +100,9 @@ __device__ __forceinline__ bool tma_rows_stage(const Frame &f, const RowMaps &mp
         constexpr int RBW = 3 * (P + 1);
         for (int h = threadIdx.x; h < N * RBW; h += blockDim.x) {
             const int i = h / RBW, r = h - i * RBW, qb = r / 3, s = r - 3 * qb;
-            const float v = (wrap && qb == nvalid) ? RW[i * 4 + s] : RB[i * WB + r];
-            SB[qb * BSR + 3 * i + nib(f.ib, s)] = v;
+            const float *src = (wrap && qb == nvalid) ? &RW[i * 4 + s] : &RB[i * WB + r];
+            if (MHD_SM(src, 4) && MHD_SM(&SB[qb * BSR + 3 * i + nib(f.ib, s)], 4))
+                SB[qb * BSR + 3 * i + nib(f.ib, s)] = *src;
         }
     }
     // frame b(3) of plane k+1 -> SK[q][i]
@@ -104,7 +110,8 @@ __device__ __forceinline__ bool tma_rows_stage(const Frame &f, const RowMaps &mp
         const int s3 = nib(f.pb, 2);
         for (int h = threadIdx.x; h < N * P; h += blockDim.x) {
             const int qq = h / N, i = h - qq * N;
-            SK[qq * KS + i] = RK[i * WK + 3 * qq + s3];
+            if (MHD_SM(&SK[qq * KS + i], 4) && MHD_SM(&RK[i * WK + 3 * qq + s3], 4))
+                SK[qq * KS + i] = RK[i * WK + 3 * qq + s3];
         }
     }
     __syncthreads();
@@ -135,9 +142,10 @@ __device__ __forceinline__ void tma_rows_writeback(const Frame &f, const RowMaps
 #pragma unroll
             for (int e = 0; e < 4; ++e) {
                 const int idx = 4 * w + e, qq = idx / 5, s = idx - 5 * qq;
-                e4[e] = qq < nvalid ? US[qq * PS + nib(f.iu, s) * CS + i] : 0.0f;
+                e4[e] = qq < nvalid && MHD_SM(&US[qq * PS + nib(f.iu, s) * CS + i], 4)
+                            ? US[qq * PS + nib(f.iu, s) * CS + i] : 0.0f;
             }
-            R4[i * (WU / 4) + w] = make_float4(e4[0], e4[1], e4[2], e4[3]);
+            if (MHD_SM(&R4[i * (WU / 4) + w], 16)) R4[i * (WU / 4) + w] = make_float4(e4[0], e4[1], e4[2], e4[3]);
         }
     }
     fence_proxy_async_smem();

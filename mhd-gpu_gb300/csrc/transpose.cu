@@ -20,6 +20,9 @@
 // shared-memory stores; other tiles move single floats.
 #include "kernels.cuh"
 
+#undef MHD_DBG_FILE
+#define MHD_DBG_FILE 6
+
 namespace mhd {
 
 struct TransposeArgs {
@@ -47,6 +50,8 @@ transpose_kernel(TransposeArgs t)
     const long long o = blockIdx.z;
     const int na = min(kTile, t.A - a0);
     const int nb = min(kTile, t.B - b0);
+    // cells of the box (the debug build's extent for global indices)
+#define MHD_TNC ((long long)t.A * t.B * t.O)
 
     if (t.vec && na == kTile && nb == kTile) {
         // u: 32 rows x 40 vectors, b: 32 rows x 24 vectors; 256 threads
@@ -56,24 +61,30 @@ transpose_kernel(TransposeArgs t)
         for (int k = 0; k < kVu; ++k) {
             const int e = threadIdx.x + 256 * k, r = e / 40, c = e - r * 40;
             const long long cell = (long long)a0 + (long long)(b0 + r) * t.sb_in + o * t.so_in;
-            lu[k] = __ldg(reinterpret_cast<const float4 *>(t.su + cell * 5) + c);
+            lu[k] = MHD_GM(t.su + cell * 5 + 4 * c + 3, t.su, 5 * MHD_TNC)
+                        ? __ldg(reinterpret_cast<const float4 *>(t.su + cell * 5) + c)
+                        : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         }
 #pragma unroll
         for (int k = 0; k < kVb; ++k) {
             const int e = threadIdx.x + 256 * k, r = e / 24, c = e - r * 24;
             const long long cell = (long long)a0 + (long long)(b0 + r) * t.sb_in + o * t.so_in;
-            lb[k] = __ldg(reinterpret_cast<const float4 *>(t.sb + cell * 3) + c);
+            lb[k] = MHD_GM(t.sb + cell * 3 + 4 * c + 3, t.sb, 3 * MHD_TNC)
+                        ? __ldg(reinterpret_cast<const float4 *>(t.sb + cell * 3) + c)
+                        : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         }
 #pragma unroll
         for (int k = 0; k < kVu; ++k) {
             const int e = threadIdx.x + 256 * k, r = e / 40, c = e - r * 40;
             float *d = tu + r * kRowU + 4 * c;
+            if (!MHD_IN(r * kRowU + 4 * c + 3, kTile * kRowU)) continue;
             d[0] = lu[k].x; d[1] = lu[k].y; d[2] = lu[k].z; d[3] = lu[k].w;
         }
 #pragma unroll
         for (int k = 0; k < kVb; ++k) {
             const int e = threadIdx.x + 256 * k, r = e / 24, c = e - r * 24;
             float *d = tb + r * kRowB + 4 * c;
+            if (!MHD_IN(r * kRowB + 4 * c + 3, kTile * kRowB)) continue;
             d[0] = lb[k].x; d[1] = lb[k].y; d[2] = lb[k].z; d[3] = lb[k].w;
         }
         __syncthreads();
@@ -86,10 +97,12 @@ transpose_kernel(TransposeArgs t)
 #pragma unroll
             for (int m = 0; m < 4; ++m) {
                 const int col = 4 * c + m, bb = col / 5, cc = col - bb * 5;
-                v[m] = tu[bb * kRowU + s * 5 + ((t.pu >> (4 * cc)) & 15u)];
+                const int x = bb * kRowU + s * 5 + ((t.pu >> (4 * cc)) & 15u);
+                v[m] = MHD_IN(x, kTile * kRowU) ? tu[x] : 0.0f;
             }
             const long long cell = (long long)b0 + (long long)(a0 + s) * t.sa_out + o * t.so_out;
-            reinterpret_cast<float4 *>(t.du + cell * 5)[c] = make_float4(v[0], v[1], v[2], v[3]);
+            if (MHD_GM(t.du + cell * 5 + 4 * c + 3, t.du, 5 * MHD_TNC))
+                reinterpret_cast<float4 *>(t.du + cell * 5)[c] = make_float4(v[0], v[1], v[2], v[3]);
         }
 #pragma unroll
         for (int k = 0; k < kVb; ++k) {
@@ -98,10 +111,12 @@ transpose_kernel(TransposeArgs t)
 #pragma unroll
             for (int m = 0; m < 4; ++m) {
                 const int col = 4 * c + m, bb = col / 3, cc = col - bb * 3;
-                v[m] = tb[bb * kRowB + s * 3 + ((t.pb >> (4 * cc)) & 15u)];
+                const int x = bb * kRowB + s * 3 + ((t.pb >> (4 * cc)) & 15u);
+                v[m] = MHD_IN(x, kTile * kRowB) ? tb[x] : 0.0f;
             }
             const long long cell = (long long)b0 + (long long)(a0 + s) * t.sa_out + o * t.so_out;
-            reinterpret_cast<float4 *>(t.db + cell * 3)[c] = make_float4(v[0], v[1], v[2], v[3]);
+            if (MHD_GM(t.db + cell * 3 + 4 * c + 3, t.db, 3 * MHD_TNC))
+                reinterpret_cast<float4 *>(t.db + cell * 3)[c] = make_float4(v[0], v[1], v[2], v[3]);
         }
         return;
     }
@@ -111,14 +126,16 @@ transpose_kernel(TransposeArgs t)
         const int r = e / (kTile * 5), col = e - r * (kTile * 5);
         if (r < nb && col < na * 5) {
             const long long cell = (long long)a0 + (long long)(b0 + r) * t.sb_in + o * t.so_in;
-            tu[r * kRowU + col] = t.su[cell * 5 + col];
+            if (MHD_IN(r * kRowU + col, kTile * kRowU) && MHD_GM(t.su + cell * 5 + col, t.su, 5 * MHD_TNC))
+                tu[r * kRowU + col] = t.su[cell * 5 + col];
         }
     }
     for (int e = threadIdx.x; e < kTile * kTile * 3; e += blockDim.x) {
         const int r = e / (kTile * 3), col = e - r * (kTile * 3);
         if (r < nb && col < na * 3) {
             const long long cell = (long long)a0 + (long long)(b0 + r) * t.sb_in + o * t.so_in;
-            tb[r * kRowB + col] = t.sb[cell * 3 + col];
+            if (MHD_IN(r * kRowB + col, kTile * kRowB) && MHD_GM(t.sb + cell * 3 + col, t.sb, 3 * MHD_TNC))
+                tb[r * kRowB + col] = t.sb[cell * 3 + col];
         }
     }
     __syncthreads();
@@ -128,7 +145,9 @@ transpose_kernel(TransposeArgs t)
         const int bb = col / 5, cc = col - bb * 5;
         if (s < na && bb < nb) {
             const long long cell = (long long)b0 + (long long)(a0 + s) * t.sa_out + o * t.so_out;
-            t.du[cell * 5 + col] = tu[bb * kRowU + s * 5 + ((t.pu >> (4 * cc)) & 15u)];
+            const int x = bb * kRowU + s * 5 + ((t.pu >> (4 * cc)) & 15u);
+            if (MHD_IN(x, kTile * kRowU) && MHD_GM(t.du + cell * 5 + col, t.du, 5 * MHD_TNC))
+                t.du[cell * 5 + col] = tu[x];
         }
     }
     for (int e = threadIdx.x; e < kTile * kTile * 3; e += blockDim.x) {
@@ -136,9 +155,12 @@ transpose_kernel(TransposeArgs t)
         const int bb = col / 3, cc = col - bb * 3;
         if (s < na && bb < nb) {
             const long long cell = (long long)b0 + (long long)(a0 + s) * t.sa_out + o * t.so_out;
-            t.db[cell * 3 + col] = tb[bb * kRowB + s * 3 + ((t.pb >> (4 * cc)) & 15u)];
+            const int x = bb * kRowB + s * 3 + ((t.pb >> (4 * cc)) & 15u);
+            if (MHD_IN(x, kTile * kRowB) && MHD_GM(t.db + cell * 3 + col, t.db, 3 * MHD_TNC))
+                t.db[cell * 3 + col] = tb[x];
         }
     }
+#undef MHD_TNC
 }
 
 cudaError_t launch_transpose(float *du, float *db, const float *su, const float *sb,

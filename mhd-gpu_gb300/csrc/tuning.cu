@@ -21,7 +21,7 @@ static std::mutex g_tile_mutex;
 static std::map<std::pair<int, int>, PencilCfg> g_tiles;
 // per host thread: a setting made on one thread changes only that thread's launches
 static thread_local int g_math = MHD_MATH_FAITHFUL;
-static thread_local int g_staging = MHD_STAGING_TMA;
+static thread_local int g_staging = MHD_STAGING_CPASYNC;
 static thread_local int g_poison = 0;
 
 // Pencils across memory are staged in rows of PPC cells, so they want many

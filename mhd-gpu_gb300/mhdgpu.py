@@ -11,7 +11,9 @@ import ctypes as C
 import os
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "lib", "libmhdgpu.so")
+# MHDGPU_LIB selects another build of the library, e.g. the debug build
+# lib/libmhdgpu_debug.so (build.py --debug)
+LIB_PATH = os.environ.get("MHDGPU_LIB") or os.path.join(HERE, "lib", "libmhdgpu.so")
 
 MHD_OK = 0
 MHD_ERR_ARG = 1
@@ -39,6 +41,7 @@ EXPORTS = [
     "mhdgpu_step_fused_workspace_bytes", "mhdgpu_step_fused",
     "mhdgpu_run_host", "mhdgpu_release_host_cache", "mhdgpu_resolve_path", "mhdgpu_path_workspace_bytes",
     "mhdgpu_set_math", "mhdgpu_set_row_staging", "mhdgpu_set_poison", "mhdgpu_set_tile", "mhdgpu_get_tile",
+    "mhdgpu_debug_build", "mhdgpu_debug_faults", "mhdgpu_debug_selftest",
     "mhdgpu_autotune", "mhdgpu_profiler_create", "mhdgpu_profiler_destroy",
     "mhdgpu_profiler_attach", "mhdgpu_profiler_reset", "mhdgpu_profiler_summary",
     "mhdgpu_diagnostics_scratch_bytes", "mhdgpu_diagnostics",
@@ -103,6 +106,9 @@ def lib() -> C.CDLL:
             "mhdgpu_set_math": (I, [I]),
             "mhdgpu_set_row_staging": (I, [I]),
             "mhdgpu_set_poison": (I, [I]),
+            "mhdgpu_debug_build": (I, []),
+            "mhdgpu_debug_faults": (I, [P, P, P, P, P, P]),
+            "mhdgpu_debug_selftest": (I, [C.c_longlong, C.c_longlong, P]),
             "mhdgpu_set_tile": (I, [I, I, I, I, I]),
             "mhdgpu_get_tile": (I, [I, I, P, P, P]),
             "mhdgpu_autotune": (I, [I, I, I, I]),
@@ -293,6 +299,39 @@ def set_row_staging(mode: int) -> int:
     if prev < 0:
         raise MhdError(MHD_ERR_ARG, lib().mhdgpu_last_error().decode())
     return prev
+
+
+# source files of the debug build's index checks, by their number in a record
+DEBUG_FILES = {1: "fluidx_reg.cuh", 2: "fluidx_kernel.cuh", 3: "advect_reg.cuh", 4: "advect_kernel.cuh",
+               5: "batch_kernel.cuh", 6: "transpose.cu", 7: "cfl_kernel.cuh", 8: "tma_rows.cuh",
+               9: "mhd_common.cuh", 10: "debug.cu"}
+DEBUG_KINDS = {1: "index", 2: "shared", 3: "global"}
+
+
+def debug_build() -> bool:
+    """True when the loaded library is the debug build (every kernel index checked)."""
+    return bool(lib().mhdgpu_debug_build())
+
+
+def debug_faults() -> dict:
+    """Synchronises the device and returns the index faults recorded by the
+    debug build since the last call: {'count', 'kind', 'file', 'line',
+    'index', 'extent'} of the first one (count 0 in the release build)."""
+    c, k, f, ln = C.c_uint(), C.c_uint(), C.c_uint(), C.c_uint()
+    i, n = C.c_longlong(), C.c_longlong()
+    _check(lib().mhdgpu_debug_faults(C.byref(c), C.byref(k), C.byref(f), C.byref(ln), C.byref(i), C.byref(n)))
+    if c.value == 0:
+        return {"count": 0}
+    return {"count": c.value, "kind": DEBUG_KINDS.get(k.value, k.value), "file": DEBUG_FILES.get(f.value, f.value),
+            "line": ln.value, "index": i.value, "extent": n.value}
+
+
+def debug_selftest(index: int, extent: int) -> bool:
+    """Checks index against extent in a one-thread kernel (mhdgpu_debug_selftest):
+    whether the check passed (always True in the release build)."""
+    r = C.c_int()
+    _check(lib().mhdgpu_debug_selftest(int(index), int(extent), C.byref(r)))
+    return bool(r.value)
 
 
 def set_poison(on: bool) -> bool:

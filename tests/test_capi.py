@@ -101,8 +101,8 @@ def test_tile_and_math_settings_without_a_gpu(L):
     assert L.mhdgpu_set_tile(2, 64, 2, 1, 1) == mhdgpu.MHD_ERR_ARG       # not a pencil kernel
     assert L.mhdgpu_set_math(7) == -1
     assert L.mhdgpu_set_math(0) == 0
+    assert L.mhdgpu_set_row_staging(mhdgpu.MHD_STAGING_TMA) == mhdgpu.MHD_STAGING_CPASYNC   # the default
     assert L.mhdgpu_set_row_staging(mhdgpu.MHD_STAGING_CPASYNC) == mhdgpu.MHD_STAGING_TMA
-    assert L.mhdgpu_set_row_staging(mhdgpu.MHD_STAGING_TMA) == mhdgpu.MHD_STAGING_CPASYNC
     assert L.mhdgpu_set_row_staging(5) == -1
     assert L.mhdgpu_autotune(0, 4, 4, 0) == mhdgpu.MHD_ERR_ARG
 
@@ -116,15 +116,15 @@ def test_settings_are_per_host_thread(L):
 
     def other():
         seen["math_before"] = L.mhdgpu_set_math(mhdgpu.MHD_MATH_FAST)
-        seen["staging_before"] = L.mhdgpu_set_row_staging(mhdgpu.MHD_STAGING_CPASYNC)
+        seen["staging_before"] = L.mhdgpu_set_row_staging(mhdgpu.MHD_STAGING_TMA)
 
     assert L.mhdgpu_set_math(mhdgpu.MHD_MATH_FP64P) == mhdgpu.MHD_MATH_FAITHFUL
     th = threading.Thread(target=other)
     th.start()
     th.join()
-    assert seen == {"math_before": mhdgpu.MHD_MATH_FAITHFUL, "staging_before": mhdgpu.MHD_STAGING_TMA}
+    assert seen == {"math_before": mhdgpu.MHD_MATH_FAITHFUL, "staging_before": mhdgpu.MHD_STAGING_CPASYNC}
     assert L.mhdgpu_set_math(mhdgpu.MHD_MATH_FAITHFUL) == mhdgpu.MHD_MATH_FP64P
-    assert L.mhdgpu_set_row_staging(mhdgpu.MHD_STAGING_TMA) == mhdgpu.MHD_STAGING_TMA
+    assert L.mhdgpu_set_row_staging(mhdgpu.MHD_STAGING_CPASYNC) == mhdgpu.MHD_STAGING_CPASYNC
 
 
 def test_workspace_sizes(L):

@@ -1,12 +1,13 @@
 """The transpose-free step with its y/z fluid tiles moved by TMA tensor copies
-(MHD_STAGING_TMA, tma_rows.cuh) against the same step with 4-byte row copies
-(MHD_STAGING_CPASYNC) and against the plain step: bit for bit.
+(MHD_STAGING_TMA, tma_rows.cuh) against the same step with the default
+staging (MHD_STAGING_CPASYNC: 16-byte quads of four pencils for full tiles,
+4-byte row copies otherwise) and against the plain step: bit for bit.
 
 The boxes cover pencils of 32, 64 and 128 cells along y and z (the lengths
 that take the TMA tile), full and partial last tiles (a j extent that is not
 a multiple of 8), the periodic j+1 column of the last tile, one- and
 two-tile planes, and a box whose row stride is not a multiple of 4 cells
-(nx = 10: the step falls back to the row copies)."""
+(nx = 10: both modes fall back to the row copies)."""
 import numpy as np
 import pytest
 
