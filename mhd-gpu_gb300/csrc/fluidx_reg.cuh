@@ -171,28 +171,34 @@ __device__ __forceinline__ void rows_vec_stage(const Frame &f, const float *u_in
     for (int un = threadIdx.x; un < units; un += blockDim.x) {
         const int Q = un / N, i = un - Q * N;
         const long long cell = kb + (long long)i * f.si + j0 + 4 * Q;
-        if (MHD_GM(u_in + cell * 5, u_in, MHD_NU(f)) && MHD_GM(u_in + cell * 5 + 19, u_in, MHD_NU(f))) {
-            const float4 *g = reinterpret_cast<const float4 *>(u_in + cell * 5);
-            float4 v[5];
+        const float *gk = b + (kpb + (long long)i * f.si + j0 + 4 * Q) * 3 + pb2;
+        if (!(MHD_GM(u_in + cell * 5, u_in, MHD_NU(f)) && MHD_GM(u_in + cell * 5 + 19, u_in, MHD_NU(f)) &&
+              MHD_GM(b + cell * 3, b, MHD_NB(f)) && MHD_GM(b + cell * 3 + 11, b, MHD_NB(f)) &&
+              MHD_GM(gk, b, MHD_NB(f)) && MHD_GM(gk + 9, b, MHD_NB(f))))
+            continue;
+        // every load of the quad first (all in flight together), then the stores
+        float4 v[5];
+        const float4 *gu = reinterpret_cast<const float4 *>(u_in + cell * 5);
 #pragma unroll
-            for (int w = 0; w < 5; ++w) v[w] = g[w];
-            rows_vec_put_u<PS>(US + 4 * Q * PS + i, v, co);
-        }
-        if (MHD_GM(b + cell * 3, b, MHD_NB(f)) && MHD_GM(b + cell * 3 + 11, b, MHD_NB(f))) {
-            const float4 *g = reinterpret_cast<const float4 *>(b + cell * 3);
-            const float4 v0 = g[0], v1 = g[1], v2 = g[2];
-            const float e[12] = {v0.x, v0.y, v0.z, v0.w, v1.x, v1.y, v1.z, v1.w, v2.x, v2.y, v2.z, v2.w};
+        for (int w = 0; w < 5; ++w) v[w] = gu[w];
+        const float4 *gb = reinterpret_cast<const float4 *>(b + cell * 3);
+        const float4 w0 = gb[0], w1 = gb[1], w2 = gb[2];
+        float kv[4];
+#pragma unroll
+        for (int x = 0; x < 4; ++x) kv[x] = gk[3 * x];
+        rows_vec_put_u<PS>(US + 4 * Q * PS + i, v, co);
+        {
+            const float e[12] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w, w2.x, w2.y, w2.z, w2.w};
             float *d = SB + 4 * Q * BSR + 3 * i;
 #pragma unroll
             for (int x = 0; x < 12; ++x)
                 if (MHD_SM(&d[(x / 3) * BSR + cb[x % 3]], 4)) d[(x / 3) * BSR + cb[x % 3]] = e[x];
         }
         {
-            const float *g = b + (kpb + (long long)i * f.si + j0 + 4 * Q) * 3 + pb2;
             float *d = SK + 4 * Q * KS + i;
 #pragma unroll
             for (int x = 0; x < 4; ++x)
-                if (MHD_SM(&d[x * KS], 4) && MHD_GM(g + 3 * x, b, MHD_NB(f))) d[x * KS] = g[3 * x];
+                if (MHD_SM(&d[x * KS], 4)) d[x * KS] = kv[x];
         }
     }
     // b of the column after the tile (column 0 when the tile ends the frame),
