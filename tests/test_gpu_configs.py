@@ -146,8 +146,8 @@ def test_ensemble64_batched_matches_oracle(gpu, oracle_lib, ensemble64):
     expression, rounded operation by operation, so turbulent boxes (where
     such operands do occur: about one van Leer quotient in 3 million, and
     now and then a total pressure whose double evaluation ends on a tie, as
-    in tests/golden/tie_pencil.npz) match as well as the smooth wave boxes.  The per-box counts and the worst errors are printed
-    with the verdict."""
+    in tests/golden/tie_pencil.npz) match as well as the smooth wave boxes.
+    The per-box counts and the worst errors are printed."""
     ens = ensemble64
     assert sum(int(np.prod(e["dims"])) for e in ens) == 27246592
     boxes = [(dev(e["u"]), dev(e["b"]), e["dims"]) for e in ens]
