@@ -427,6 +427,37 @@ def profiled(fn, steps, stream, flush):
     return s
 
 
+TUNE_CACHE = None   # --tune-cache
+
+
+def tune_tiles(n, math_mode):
+    """mhdgpu_autotune for an n^3 box, or its picks from --tune-cache when the
+    cache holds them for this device (then saved there after tuning); returns
+    where the shapes came from."""
+    import mhdgpu
+    path = os.path.join(TUNE_CACHE, f"tiles_{n}_math{math_mode}.json") if TUNE_CACHE else None
+    if path and os.path.exists(path) and mhdgpu.tile_cache_load(path) > 0:
+        return "tile cache (mhdgpu_tile_cache_load)"
+    mhdgpu.autotune(n, n, n, math_mode)
+    if path:
+        os.makedirs(TUNE_CACHE, exist_ok=True)
+        mhdgpu.tile_cache_save(path)
+    return "mhdgpu_autotune"
+
+
+def tune_batch(bt, stream):
+    """mhdgpu_batch_tune, or the schedule from --tune-cache when it was saved
+    for this batch on this device model (then saved there after tuning)."""
+    path = os.path.join(TUNE_CACHE, "batch_schedule.json") if TUNE_CACHE else None
+    if path and os.path.exists(path) and bt.load_schedule(path):
+        return "schedule cache (mhdgpu_batch_schedule_load)"
+    bt.tune(stream=stream)
+    if path:
+        os.makedirs(TUNE_CACHE, exist_ok=True)
+        bt.save_schedule(path)
+    return "mhdgpu_batch_tune"
+
+
 def single_box(n, K, W, stream, flush, world, dev, tune, math_mode):
     """The 128^3 (n^3) single-box numbers: fused and plain steps, the fluidx
     roofline and the e2e host-buffer call."""
@@ -434,15 +465,12 @@ def single_box(n, K, W, stream, flush, world, dev, tune, math_mode):
     import ics
     import mhdgpu
     ncell = n ** 3
-    if tune:
-        picks = mhdgpu.autotune(n, n, n, math_mode)
-    else:
-        picks = {(k, n, r): mhdgpu.get_tile(k, n, rows=r) for k in ("fluidx", "advectbyzx")
-                 for r in (False, True)}
+    tiles_from = tune_tiles(n, math_mode) if tune else "defaults"
+    picks = {(k, n, r): mhdgpu.get_tile(k, n, rows=r) for k in ("fluidx", "advectbyzx") for r in (False, True)}
     u0, b0 = ics.alfven_oblique(n)
     res = {"workload": f"alfven_diag_{n}", "box": [n, n, n],
            "tiles": {f"{k}@{m}{'/rows' if r else ''}": list(v) for (k, m, r), v in picks.items()},
-           "tiles_from": "mhdgpu_autotune" if tune else "defaults"}
+           "tiles_from": tiles_from}
     for path, name in ((mhdgpu.MHD_PATH_FUSED, "fused"), (mhdgpu.MHD_PATH_PLAIN, "plain")):
         du = torch.from_numpy(u0).to(dev)
         db = torch.from_numpy(b0).to(dev)
@@ -511,7 +539,8 @@ def ensemble_bench(ens, K, W, stream, flush, world, dev, tune, total_cells):
     cells = int(sum(int(np.prod(d)) for d in dims))
     boxes = [(torch.from_numpy(e["u"]).to(dev), torch.from_numpy(e["b"]).to(dev), e["dims"]) for e in ens]
     bt = mhdgpu.Batch(boxes, cfl_number=CFL, cfl_mode=mhdgpu.MHD_CFL_C)
-    sched = bt.tune(stream=stream) if tune else [bt.get_schedule(a) for a in range(3)]
+    sched_from = tune_batch(bt, stream) if tune else "defaults"
+    sched = [bt.get_schedule(a) for a in range(3)]
 
     def step():
         # one step per call, continuing the previous one (the CFL speed comes
@@ -537,7 +566,7 @@ def ensemble_bench(ens, K, W, stream, flush, world, dev, tune, total_cells):
     pass_ach = SWEEP_PASS_BYTES_PER_CELL * cells / avg_s / 1e9
     tot_ms = sum(v[2] for v in summ.values())
     res = {"value": value, "ms_per_step": secs / K * 1e3, "cells": cells, "schedule": sched,
-           "schedule_from": "mhdgpu_batch_tune" if tune else "defaults", "wall": wall,
+           "schedule_from": sched_from, "wall": wall,
            "kernel_time_ms_per_step": {k: v[2] / ksteps for k, v in summ.items()},
            "kernel_launches_per_step": {k: v[1] / ksteps for k, v in summ.items()},
            "health": health,
@@ -651,10 +680,15 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--math", default="faithful", choices=["faithful", "fast"])
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuners (default tiles)")
+    ap.add_argument("--tune-cache", default=None,
+                    help="directory of the autotuners' JSON picks: reused when they match this device and "
+                         "workload, written after tuning otherwise")
     ap.add_argument("--headline-only", action="store_true",
                     help="time the headline path only (no secondary paths, e2e or CPU baseline); "
                          "for profiler captures")
     args = ap.parse_args()
+    global TUNE_CACHE
+    TUNE_CACHE = args.tune_cache
     n, K, W = args.n, args.steps, max(3, args.warmup)
     ens_mode = args.workload == "ensemble64"
     if args.impl == "ours":
@@ -717,7 +751,7 @@ def main():
             boxes = [(torch.from_numpy(e["u"]).to(dev), torch.from_numpy(e["b"]).to(dev), e["dims"]) for e in ens]
             bt = mhdgpu.Batch(boxes, cfl_number=CFL, cfl_mode=mhdgpu.MHD_CFL_C)
             if tune:
-                bt.tune(stream=stream)
+                tune_batch(bt, stream)
             g = capture(lambda: bt.advance(1, stream=stream, resume=True), stream, 2)
             cells = total
         else:
@@ -726,7 +760,7 @@ def main():
             work = torch.empty(mhdgpu.step_workspace_bytes(n, n, n, 1), dtype=torch.uint8, device=dev)
             clock = mhdgpu.new_clock(device=dev)
             if tune:
-                mhdgpu.autotune(n, n, n, math_mode)
+                tune_tiles(n, math_mode)
             started = [False]
 
             def one_step():

@@ -314,6 +314,15 @@ int mhdgpu_get_tile(int kclass, int n, int *cpl, int *wpp, int *ppc);
  * synchronises the device.  Not for use under stream capture. */
 int mhdgpu_autotune(int nx, int ny, int nz, int math);
 
+/* The autotuner's picks as JSON, so a tuned configuration is reused without
+ * timing it again.  mhdgpu_tile_cache_save writes every shape set in this
+ * process's table (by mhdgpu_set_tile or mhdgpu_autotune) with the current
+ * device's name; mhdgpu_tile_cache_load sets the shapes a file holds and
+ * reports how many in *applied (0 when the file was written on another
+ * device model).  MHD_ERR_ARG for an unreadable or malformed file. */
+int mhdgpu_tile_cache_save(const char *path);
+int mhdgpu_tile_cache_load(const char *path, int *applied);
+
 /* ------------------------------------------------------------------------
  * FP64 diagnostics of a state (the reference prints float sums from the host,
  * Heterogeneous_MHD/C/check_value.c:22-79).  d_out (device, 8 doubles):
@@ -424,6 +433,15 @@ int mhdgpu_batch_get_schedule(const mhdgpu_batch *bt, int axis, int *threads, in
  * already enqueued on any stream finish first); synchronises.  Not under
  * stream capture. */
 int mhdgpu_batch_tune(mhdgpu_batch *bt, mhdgpu_stream_t stream);
+
+/* The batch's schedule (threads and CTAs-per-SM cap of each axis, e.g. as
+ * mhdgpu_batch_tune left it) as JSON, with the device's name and a signature
+ * of the batch (its boxes' sizes in order and the calling thread's arithmetic
+ * policy).  mhdgpu_batch_schedule_load applies a file's schedule when device
+ * and signature match (*applied = 1; a schedule change as by
+ * mhdgpu_batch_set_schedule), else leaves the batch as it is (*applied = 0). */
+int mhdgpu_batch_schedule_save(const mhdgpu_batch *bt, const char *path);
+int mhdgpu_batch_schedule_load(mhdgpu_batch *bt, const char *path, int *applied);
 /* Failure-path test hook: from the next step on, the first dependency wait of
  * box 0 in the first sweep waits for one item more than exist, so it gives up
  * after its limit (about two seconds): the box's health gets MHD_HEALTH_STALL,

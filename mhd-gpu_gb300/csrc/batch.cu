@@ -11,6 +11,7 @@
 
 #include "batch_kernel.cuh"
 #include "profiler.cuh"
+#include "tunecache.h"
 
 namespace mhd {
 
@@ -769,6 +770,68 @@ int mhdgpu_batch_get_schedule(const mhdgpu_batch *bt, int axis, int *threads, in
     if (!bt || axis < 0 || axis > 2) return bfail(MHD_ERR_ARG, "mhdgpu_batch_get_schedule: bad argument");
     if (threads) *threads = bt->threads[axis];
     if (ctas_per_sm) *ctas_per_sm = bt->cps[axis];
+    return MHD_OK;
+}
+
+// the batch's signature for the schedule cache: its boxes' sizes in order and
+// the arithmetic policy of the calling thread (the class kernels differ by it)
+static unsigned long long batch_signature(const mhdgpu_batch *bt)
+{
+    Fnv64 h;
+    h.add(bt->nbox);
+    for (const BoxDesc &d : bt->box) {
+        h.add(d.nx);
+        h.add(d.ny);
+        h.add(d.nz);
+    }
+    h.add(math_mode());
+    return h.h;
+}
+
+int mhdgpu_batch_schedule_save(const mhdgpu_batch *bt, const char *path)
+{
+    if (!bt || !path) return bfail(MHD_ERR_ARG, "mhdgpu_batch_schedule_save: null argument");
+    FILE *f = fopen(path, "w");
+    if (!f) return bfail(MHD_ERR_ARG, "mhdgpu_batch_schedule_save: cannot open the file");
+    fprintf(f, "{\n  \"format\": \"mhdgpu batch schedule 1\",\n  \"device\": \"%s\",\n"
+               "  \"signature\": \"%016llx\",\n  \"boxes\": %d,\n  \"schedule\": [",
+            tune_device_name().c_str(), batch_signature(bt), bt->nbox);
+    for (int a = 0; a < 3; ++a)
+        fprintf(f, "%s\n    {\"axis\": %d, \"threads\": %d, \"ctas_per_sm\": %d}", a ? "," : "", a,
+                bt->threads[a], bt->cps[a]);
+    fprintf(f, "\n  ]\n}\n");
+    if (fclose(f) != 0) return bfail(MHD_ERR_ARG, "mhdgpu_batch_schedule_save: write failed");
+    return MHD_OK;
+}
+
+int mhdgpu_batch_schedule_load(mhdgpu_batch *bt, const char *path, int *applied)
+{
+    if (applied) *applied = 0;
+    if (!bt || !path) return bfail(MHD_ERR_ARG, "mhdgpu_batch_schedule_load: null argument");
+    std::string text, fmt, dev, sig;
+    if (!read_text(path, text)) return bfail(MHD_ERR_ARG, "mhdgpu_batch_schedule_load: cannot read the file");
+    if (!json_string(text, "format", fmt) || fmt != "mhdgpu batch schedule 1" || !json_string(text, "device", dev) ||
+        !json_string(text, "signature", sig))
+        return bfail(MHD_ERR_ARG, "mhdgpu_batch_schedule_load: not a batch schedule");
+    char mine[32];
+    snprintf(mine, sizeof mine, "%016llx", batch_signature(bt));
+    if (!same_device(dev, tune_device_name()) || sig != mine) return MHD_OK;   // another device or batch
+    int thr[3], cps[3], seen = 0;
+    for (size_t p = text.find("{\"axis\""); p != std::string::npos && seen < 3; p = text.find("{\"axis\"", p + 1)) {
+        int a, t, c;
+        if (sscanf(text.c_str() + p, " { \"axis\" : %d , \"threads\" : %d , \"ctas_per_sm\" : %d }", &a, &t, &c) != 3 ||
+            a != seen)
+            return bfail(MHD_ERR_ARG, "mhdgpu_batch_schedule_load: malformed schedule");
+        thr[a] = t;
+        cps[a] = c;
+        ++seen;
+    }
+    if (seen != 3) return bfail(MHD_ERR_ARG, "mhdgpu_batch_schedule_load: malformed schedule");
+    for (int a = 0; a < 3; ++a) {
+        const int st = mhdgpu_batch_set_schedule(bt, a, thr[a], cps[a]);
+        if (st != MHD_OK) return st;
+    }
+    if (applied) *applied = 1;
     return MHD_OK;
 }
 

@@ -14,6 +14,7 @@
 #include <vector>
 
 #include "kernels.cuh"
+#include "tunecache.h"
 
 namespace mhd {
 
@@ -141,6 +142,69 @@ int mhdgpu_get_tile(int kclass, int n, int *cpl, int *wpp, int *ppc)
     if (cpl) *cpl = c.cpl;
     if (wpp) *wpp = c.wpp;
     if (ppc) *ppc = c.ppc;
+    return MHD_OK;
+}
+
+int mhdgpu_tile_cache_save(const char *path)
+{
+    if (!path) {
+        set_last_error("mhdgpu_tile_cache_save: null path");
+        return MHD_ERR_ARG;
+    }
+    std::map<std::pair<int, int>, PencilCfg> tiles;
+    {
+        std::lock_guard<std::mutex> lock(g_tile_mutex);
+        tiles = g_tiles;
+    }
+    FILE *f = fopen(path, "w");
+    if (!f) {
+        set_last_error("mhdgpu_tile_cache_save: cannot open the file");
+        return MHD_ERR_ARG;
+    }
+    fprintf(f, "{\n  \"format\": \"mhdgpu tile cache 1\",\n  \"device\": \"%s\",\n  \"tiles\": [",
+            tune_device_name().c_str());
+    bool first = true;
+    for (const auto &t : tiles) {
+        fprintf(f, "%s\n    {\"kclass\": %d, \"n\": %d, \"cpl\": %d, \"wpp\": %d, \"ppc\": %d}",
+                first ? "" : ",", t.first.first, t.first.second, t.second.cpl, t.second.wpp, t.second.ppc);
+        first = false;
+    }
+    fprintf(f, "\n  ]\n}\n");
+    const bool ok = fclose(f) == 0;
+    if (!ok) {
+        set_last_error("mhdgpu_tile_cache_save: write failed");
+        return MHD_ERR_ARG;
+    }
+    return MHD_OK;
+}
+
+int mhdgpu_tile_cache_load(const char *path, int *applied)
+{
+    if (applied) *applied = 0;
+    std::string text, dev;
+    if (!path || !read_text(path, text)) {
+        set_last_error("mhdgpu_tile_cache_load: cannot read the file");
+        return MHD_ERR_ARG;
+    }
+    std::string fmt;
+    if (!json_string(text, "format", fmt) || fmt != "mhdgpu tile cache 1" || !json_string(text, "device", dev)) {
+        set_last_error("mhdgpu_tile_cache_load: not a tile cache");
+        return MHD_ERR_ARG;
+    }
+    if (!same_device(dev, tune_device_name())) return MHD_OK;   // tuned on another device: nothing applies
+    int count = 0;
+    for (size_t p = text.find("{\"kclass\""); p != std::string::npos; p = text.find("{\"kclass\"", p + 1)) {
+        int kc, n, cpl, wpp, ppc;
+        if (sscanf(text.c_str() + p, " { \"kclass\" : %d , \"n\" : %d , \"cpl\" : %d , \"wpp\" : %d , \"ppc\" : %d }",
+                   &kc, &n, &cpl, &wpp, &ppc) != 5) {
+            set_last_error("mhdgpu_tile_cache_load: malformed entry");
+            return MHD_ERR_ARG;
+        }
+        const int st = mhdgpu_set_tile(kc, n, cpl, wpp, ppc);
+        if (st != MHD_OK) return st;
+        ++count;
+    }
+    if (applied) *applied = count;
     return MHD_OK;
 }
 

@@ -42,7 +42,7 @@ EXPORTS = [
     "mhdgpu_run_host", "mhdgpu_release_host_cache", "mhdgpu_resolve_path", "mhdgpu_path_workspace_bytes",
     "mhdgpu_set_math", "mhdgpu_set_row_staging", "mhdgpu_set_poison", "mhdgpu_set_tile", "mhdgpu_get_tile",
     "mhdgpu_debug_build", "mhdgpu_debug_faults", "mhdgpu_debug_selftest",
-    "mhdgpu_autotune", "mhdgpu_profiler_create", "mhdgpu_profiler_destroy",
+    "mhdgpu_autotune", "mhdgpu_tile_cache_save", "mhdgpu_tile_cache_load", "mhdgpu_profiler_create", "mhdgpu_profiler_destroy",
     "mhdgpu_profiler_attach", "mhdgpu_profiler_reset", "mhdgpu_profiler_summary",
     "mhdgpu_diagnostics_scratch_bytes", "mhdgpu_diagnostics",
     "mhdgpu_read_state", "mhdgpu_write_state", "mhdgpu_write_result", "mhdgpu_write_check",
@@ -50,6 +50,7 @@ EXPORTS = [
     "mhdgpu_batch_advance", "mhdgpu_batch_resume", "mhdgpu_batch_run_host", "mhdgpu_batch_read_clocks",
     "mhdgpu_batch_set_schedule",
     "mhdgpu_batch_get_schedule", "mhdgpu_batch_tune", "mhdgpu_batch_inject_stall",
+    "mhdgpu_batch_schedule_save", "mhdgpu_batch_schedule_load",
     # include/mhdgpu_compat.h
     "fluidx", "advectbyzx", "transpose12", "transpose13", "calcfl", "copy_matrix",
     "mhdgpu_compat_status",
@@ -112,6 +113,8 @@ def lib() -> C.CDLL:
             "mhdgpu_set_tile": (I, [I, I, I, I, I]),
             "mhdgpu_get_tile": (I, [I, I, P, P, P]),
             "mhdgpu_autotune": (I, [I, I, I, I]),
+            "mhdgpu_tile_cache_save": (I, [C.c_char_p]),
+            "mhdgpu_tile_cache_load": (I, [C.c_char_p, P]),
             "mhdgpu_profiler_create": (I, [P, I]),
             "mhdgpu_profiler_destroy": (I, [P]),
             "mhdgpu_profiler_attach": (I, [P]),
@@ -133,6 +136,8 @@ def lib() -> C.CDLL:
             "mhdgpu_batch_set_schedule": (I, [P, I, I, I]),
             "mhdgpu_batch_get_schedule": (I, [P, I, P, P]),
             "mhdgpu_batch_tune": (I, [P, P]),
+            "mhdgpu_batch_schedule_save": (I, [P, C.c_char_p]),
+            "mhdgpu_batch_schedule_load": (I, [P, C.c_char_p, P]),
             "mhdgpu_batch_inject_stall": (I, [P]),
             "calcfl": (F, [P, P, P, P, P]),
             "cfl_": (F, [P, P, P, P, P]),
@@ -368,6 +373,18 @@ def autotune(nx: int, ny: int, nz: int, math: int = MHD_MATH_FAITHFUL):
     return out
 
 
+def tile_cache_save(path: str) -> None:
+    """Write the tile shapes set in this process (mhdgpu_tile_cache_save)."""
+    _check(lib().mhdgpu_tile_cache_save(os.fsencode(path)))
+
+
+def tile_cache_load(path: str) -> int:
+    """Set the tile shapes a cache file holds for this device; returns how many."""
+    n = C.c_int()
+    _check(lib().mhdgpu_tile_cache_load(os.fsencode(path), C.byref(n)))
+    return n.value
+
+
 class Profiler:
     """Per-kernel-class device time from CUDA events (mhdgpu_profiler_*).
 
@@ -513,6 +530,16 @@ class Batch:
         t, c = C.c_int(), C.c_int()
         _check(lib().mhdgpu_batch_get_schedule(self.h, int(axis), C.byref(t), C.byref(c)))
         return t.value, c.value
+
+    def save_schedule(self, path):
+        """Write the schedule with the batch's signature (mhdgpu_batch_schedule_save)."""
+        _check(lib().mhdgpu_batch_schedule_save(self.h, os.fsencode(path)))
+
+    def load_schedule(self, path) -> bool:
+        """Apply a saved schedule if it was made for this batch on this device model."""
+        ok = C.c_int()
+        _check(lib().mhdgpu_batch_schedule_load(self.h, os.fsencode(path), C.byref(ok)))
+        return bool(ok.value)
 
     def tune(self, stream=None):
         """Autotune the block schedule per axis; returns [(threads, ctas_per_sm)] * 3."""

@@ -205,3 +205,34 @@ def test_diagnostics_arguments_without_a_gpu(L):
     assert L.mhdgpu_set_math(mhdgpu.MHD_MATH_FP64P) == mhdgpu.MHD_MATH_FAITHFUL
     assert L.mhdgpu_set_math(mhdgpu.MHD_MATH_FAITHFUL) == mhdgpu.MHD_MATH_FP64P
     assert L.mhdgpu_set_math(3) == -1
+
+
+def test_tile_cache_round_trip(L, tmp_path):
+    """mhdgpu_tile_cache_save / _load: the shapes set in the table come back
+    from the JSON file; a file recorded on another device model applies
+    nothing; a malformed file is an argument error."""
+    import json
+    import mhdgpu
+    f, r = mhdgpu.KCLASS["fluidx"], mhdgpu.KCLASS["fluidx"] | 16
+    assert L.mhdgpu_set_tile(f, 200, 4, 2, 1) == 0
+    assert L.mhdgpu_set_tile(r, 64, 2, 1, 8) == 0
+    p = tmp_path / "tiles.json"
+    mhdgpu.tile_cache_save(str(p))
+    rec = json.load(open(p))
+    assert rec["format"] == "mhdgpu tile cache 1"
+    assert {"kclass": f, "n": 200, "cpl": 4, "wpp": 2, "ppc": 1} in rec["tiles"]
+    assert L.mhdgpu_set_tile(f, 200, 2, 4, 1) == 0                        # changed after the save
+    assert mhdgpu.tile_cache_load(str(p)) == len(rec["tiles"])
+    assert mhdgpu.get_tile("fluidx", 200) == (4, 2, 1)
+    assert mhdgpu.get_tile("fluidx", 64, rows=True) == (2, 1, 8)
+    other = dict(rec, device="some other GPU")
+    q = tmp_path / "other.json"
+    json.dump(other, open(q, "w"))
+    if rec["device"]:
+        assert mhdgpu.tile_cache_load(str(q)) == 0
+    bad = tmp_path / "bad.json"
+    bad.write_text('{"format": "mhdgpu tile cache 1", "device": "", "tiles": [{"kclass": 0, "n": }]}')
+    with pytest.raises(mhdgpu.MhdError):
+        mhdgpu.tile_cache_load(str(bad))
+    with pytest.raises(mhdgpu.MhdError):
+        mhdgpu.tile_cache_load(str(tmp_path / "missing.json"))

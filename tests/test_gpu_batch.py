@@ -450,3 +450,40 @@ def test_batch_wait_timeout_is_reported_and_context_survives(gpu):
     ref = _per_box(gpu, states, dims, 2, 0.7)
     got = _batched(gpu, states, dims, 2, 0.7)
     _same(got, ref)
+
+
+def test_batch_schedule_cache(gpu, tmp_path):
+    """mhdgpu_batch_schedule_save / _load: a saved schedule applies to a batch
+    of the same boxes (same signature) and leaves a batch of other boxes as it
+    is; the reloaded schedule steps bit for bit like the original."""
+    import json
+    dims = [(32, 48, 20), (16, 96, 8), (48, 32, 64)]
+    states = _states(dims)
+    boxes = [(dev(u), dev(b), d) for (u, b), d in zip(states, dims)]
+    bt = gpu.Batch(boxes, cfl_number=0.7)
+    bt.set_schedule(0, 128, 4)
+    bt.set_schedule(2, 64, 2)
+    p = tmp_path / "schedule.json"
+    bt.save_schedule(str(p))
+    rec = json.load(open(p))
+    assert rec["format"] == "mhdgpu batch schedule 1" and rec["boxes"] == 3
+    assert rec["schedule"][0] == {"axis": 0, "threads": 128, "ctas_per_sm": 4}
+    bt.advance(2)
+    ref = [(host(u), host(b)) for u, b, _ in boxes]
+    bt.close()
+    boxes2 = [(dev(u), dev(b), d) for (u, b), d in zip(states, dims)]
+    bt2 = gpu.Batch(boxes2, cfl_number=0.7)
+    assert bt2.get_schedule(0) != (128, 4) or bt2.get_schedule(2) != (64, 2)
+    assert bt2.load_schedule(str(p))
+    assert bt2.get_schedule(0) == (128, 4) and bt2.get_schedule(2) == (64, 2)
+    assert bt2.get_schedule(1) == tuple((rec["schedule"][1]["threads"], rec["schedule"][1]["ctas_per_sm"]))
+    bt2.advance(2)
+    for (ru, rb), (u, b, _) in zip(ref, boxes2):
+        assert bits_equal(host(u), ru) and bits_equal(host(b), rb)
+    bt2.close()
+    other = [(dev(u), dev(b), d) for (u, b), d in zip(_states(dims[:2]), dims[:2])]
+    bt3 = gpu.Batch(other, cfl_number=0.7)
+    before = [bt3.get_schedule(a) for a in range(3)]
+    assert not bt3.load_schedule(str(p))
+    assert [bt3.get_schedule(a) for a in range(3)] == before
+    bt3.close()
