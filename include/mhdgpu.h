@@ -301,7 +301,9 @@ int mhdgpu_debug_selftest(long long index, long long extent, int *in_bounds);
  * memory -- the y and z sweeps of mhdgpu_step_fused) for pencils of length n:
  * cpl cells per thread, wpp warps per pencil, ppc pencils per CTA;
  * n <= 32*wpp*cpl and 32*wpp*ppc <= 256.  mhdgpu_set_tile overrides the
- * default table; mhdgpu_get_tile reports the shape in use.  Compiled shapes
+ * default table; mhdgpu_get_tile reports the shape in use.  The table is per
+ * host thread, like the settings above (mhdgpu_autotune and
+ * mhdgpu_tile_cache_load fill the calling thread's).  Compiled shapes
  * (cpl,wpp): (1,1) (2,1) (4,1) (1,2) (2,2) (4,2) (1,4) (2,4) (4,4) (2,8) (4,8). */
 #define MHD_TILE_ROWS       16
 int mhdgpu_set_tile(int kclass, int n, int cpl, int wpp, int ppc);

@@ -1,8 +1,8 @@
 // tuning.cu - tile-shape table, arithmetic policy and the autotuner.
 //
 // The pencil kernels take their team shape (cells per thread, warps per
-// pencil, pencils per CTA) from a process-wide table keyed by kernel class
-// and pencil length.  The default is a fixed table (fluidx_pick,
+// pencil, pencils per CTA) from a table keyed by kernel class and pencil
+// length, one per host thread like the other settings.  The default is a fixed table (fluidx_pick,
 // advect_pick); mhdgpu_autotune measures every compiled shape with CUDA events
 // on a synthetic state of the caller's box and records the fastest.
 #include <cuda_runtime.h>
@@ -18,8 +18,7 @@
 
 namespace mhd {
 
-static std::mutex g_tile_mutex;
-static std::map<std::pair<int, int>, PencilCfg> g_tiles;
+static thread_local std::map<std::pair<int, int>, PencilCfg> g_tiles;
 // per host thread: a setting made on one thread changes only that thread's launches
 static thread_local int g_math = MHD_MATH_FAITHFUL;
 static thread_local int g_staging = MHD_STAGING_CPASYNC;
@@ -45,7 +44,6 @@ static int tile_key(int kclass, bool rows) { return kclass | (rows ? MHD_TILE_RO
 PencilCfg pencil_cfg(int kclass, int n, bool rows)
 {
     {
-        std::lock_guard<std::mutex> lock(g_tile_mutex);
         auto it = g_tiles.find({tile_key(kclass, rows), n});
         if (it != g_tiles.end()) return it->second;
     }
@@ -127,7 +125,6 @@ int mhdgpu_set_tile(int kclass, int n, int cpl, int wpp, int ppc)
         set_last_error("mhdgpu_set_tile: shape not compiled or does not cover the pencil");
         return MHD_ERR_ARG;
     }
-    std::lock_guard<std::mutex> lock(g_tile_mutex);
     g_tiles[{kclass, n}] = c;
     return MHD_OK;
 }
@@ -151,11 +148,7 @@ int mhdgpu_tile_cache_save(const char *path)
         set_last_error("mhdgpu_tile_cache_save: null path");
         return MHD_ERR_ARG;
     }
-    std::map<std::pair<int, int>, PencilCfg> tiles;
-    {
-        std::lock_guard<std::mutex> lock(g_tile_mutex);
-        tiles = g_tiles;
-    }
+    const std::map<std::pair<int, int>, PencilCfg> tiles = g_tiles;
     FILE *f = fopen(path, "w");
     if (!f) {
         set_last_error("mhdgpu_tile_cache_save: cannot open the file");
@@ -289,10 +282,7 @@ int mhdgpu_autotune(int nx, int ny, int nz, int math)
                     }
                     if (ms_best < best) { best = ms_best; best_cfg = c; }
                 }
-                if (ret == MHD_OK) {
-                    std::lock_guard<std::mutex> lock(g_tile_mutex);
-                    g_tiles[{tile_key(kclass, rows), n}] = best_cfg;
-                }
+                if (ret == MHD_OK) g_tiles[{tile_key(kclass, rows), n}] = best_cfg;
             }
         }
     }

@@ -108,8 +108,8 @@ def test_tile_and_math_settings_without_a_gpu(L):
 
 
 def test_settings_are_per_host_thread(L):
-    """The arithmetic policy and the row staging set on one thread leave every
-    other thread's launches as they were."""
+    """The arithmetic policy, the row staging and the tile table set on one
+    thread leave every other thread's launches as they were."""
     import threading
     import mhdgpu
     seen = {}
@@ -117,12 +117,18 @@ def test_settings_are_per_host_thread(L):
     def other():
         seen["math_before"] = L.mhdgpu_set_math(mhdgpu.MHD_MATH_FAST)
         seen["staging_before"] = L.mhdgpu_set_row_staging(mhdgpu.MHD_STAGING_TMA)
+        seen["set_tile"] = L.mhdgpu_set_tile(0, 96, 4, 1, 2)
+        seen["tile_there"] = mhdgpu.get_tile("fluidx", 96)
 
     assert L.mhdgpu_set_math(mhdgpu.MHD_MATH_FP64P) == mhdgpu.MHD_MATH_FAITHFUL
+    here = mhdgpu.get_tile("fluidx", 96)
+    assert here != (4, 1, 2)
     th = threading.Thread(target=other)
     th.start()
     th.join()
-    assert seen == {"math_before": mhdgpu.MHD_MATH_FAITHFUL, "staging_before": mhdgpu.MHD_STAGING_CPASYNC}
+    assert seen == {"math_before": mhdgpu.MHD_MATH_FAITHFUL, "staging_before": mhdgpu.MHD_STAGING_CPASYNC,
+                    "set_tile": 0, "tile_there": (4, 1, 2)}
+    assert mhdgpu.get_tile("fluidx", 96) == here          # only the other thread's table changed
     assert L.mhdgpu_set_math(mhdgpu.MHD_MATH_FAITHFUL) == mhdgpu.MHD_MATH_FP64P
     assert L.mhdgpu_set_row_staging(mhdgpu.MHD_STAGING_CPASYNC) == mhdgpu.MHD_STAGING_CPASYNC
 
