@@ -167,10 +167,12 @@ int mhdgpu_step_fused(float *u, float *b, int nx, int ny, int nz, const float *d
 #define MHD_PATH_AUTO       2   /* the faster of the two for the box (mhdgpu_resolve_path) */
 
 /* The path MHD_PATH_AUTO takes for an nx*ny*nz box: MHD_PATH_FUSED when
- * every y and z pencil has at most 128 cells, else MHD_PATH_PLAIN (measured
- * on GB300: the transpose-free step is 1.27x faster at 32^3 and even with
- * the plain one at 64^3-128^3; the plain step, whose transposes run near the
- * copy bandwidth, is 1.09x faster at 256^3 and 1.71x at 512^3).
+ * every y and z pencil has at most 48 cells, else MHD_PATH_PLAIN (measured
+ * on GB300 with default tiles: the transpose-free step takes 0.82-0.89 of
+ * the plain step's time at 32^3, 48^3 and 128x32x32, the same at 64^3 and
+ * 96^3, and 1.03-1.10 of it from 128^3 up and wherever a y or z pencil is 64
+ * cells or longer in a larger box; the plain step's transposes run near the
+ * copy bandwidth and leave every sweep on contiguous pencils).
  * mhdgpu_path_workspace_bytes sizes the workspace of a path (MHD_PATH_AUTO:
  * of the path it takes). */
 int mhdgpu_resolve_path(int nx, int ny, int nz);

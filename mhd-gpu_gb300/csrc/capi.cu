@@ -316,7 +316,7 @@ static int step_fused(float *u, float *b, int nx, int ny, int nz, const float *d
 
 int mhdgpu_resolve_path(int nx, int ny, int nz)
 {
-    return (ny <= 128 && nz <= 128) ? MHD_PATH_FUSED : MHD_PATH_PLAIN;
+    return (ny <= 48 && nz <= 48) ? MHD_PATH_FUSED : MHD_PATH_PLAIN;
 }
 
 size_t mhdgpu_path_workspace_bytes(int nx, int ny, int nz, int path)

@@ -145,10 +145,11 @@ def test_path_choice_and_host_entries_without_a_gpu(L):
     argument checks, all answered on the host."""
     import mhdgpu
     fused, plain, auto = mhdgpu.MHD_PATH_FUSED, mhdgpu.MHD_PATH_PLAIN, mhdgpu.MHD_PATH_AUTO
-    assert L.mhdgpu_resolve_path(128, 128, 128) == fused
-    assert L.mhdgpu_resolve_path(512, 96, 64) == fused        # x pencils are always contiguous
+    assert L.mhdgpu_resolve_path(48, 48, 48) == fused
+    assert L.mhdgpu_resolve_path(512, 32, 48) == fused        # x pencils are always contiguous
+    assert L.mhdgpu_resolve_path(128, 128, 128) == plain
     assert L.mhdgpu_resolve_path(64, 256, 64) == plain
-    assert L.mhdgpu_resolve_path(64, 64, 129) == plain
+    assert L.mhdgpu_resolve_path(32, 32, 49) == plain
     for dims in ((128, 128, 128), (32, 256, 16)):
         want = (L.mhdgpu_step_fused_workspace_bytes(*dims) if L.mhdgpu_resolve_path(*dims) == fused
                 else L.mhdgpu_step_workspace_bytes(*dims))

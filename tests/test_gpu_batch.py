@@ -295,11 +295,12 @@ def test_batch_resume_equals_one_call(gpu):
 
 def test_auto_path_resolves_and_matches(gpu):
     """MHD_PATH_AUTO takes the transpose-free step for boxes whose y and z
-    pencils are at most 128 cells, the plain step otherwise, and ends where
+    pencils are at most 48 cells, the plain step otherwise, and ends where
     the path it resolves to ends (the two paths are bit-identical)."""
     import torch
-    assert gpu.resolve_path(64, 128, 96) == gpu.MHD_PATH_FUSED
-    assert gpu.resolve_path(256, 128, 32) == gpu.MHD_PATH_FUSED
+    assert gpu.resolve_path(64, 48, 32) == gpu.MHD_PATH_FUSED
+    assert gpu.resolve_path(256, 16, 48) == gpu.MHD_PATH_FUSED
+    assert gpu.resolve_path(64, 128, 96) == gpu.MHD_PATH_PLAIN
     assert gpu.resolve_path(16, 256, 32) == gpu.MHD_PATH_PLAIN
     assert gpu.resolve_path(16, 8, 200) == gpu.MHD_PATH_PLAIN
     assert gpu.resolve_path(512, 512, 512) == gpu.MHD_PATH_PLAIN
