@@ -165,7 +165,10 @@ __device__ __forceinline__ void batch_b1(const AdvectArgs &a, long long c0, int 
 {
     const unsigned ncell = (unsigned)(a.f.npen * a.f.n);
     const unsigned c1 = min((unsigned)c0 + (unsigned)cells, ncell);
-    for (unsigned c = (unsigned)c0 + threadIdx.x; c < c1; c += blockDim.x) advect_b1_cell(a, c);
+    const unsigned st = blockDim.x;
+    unsigned c = (unsigned)c0 + threadIdx.x;
+    for (; c + 3 * st < c1; c += 4 * st) advect_b1_cell4(a, c, st);   // four cells' loads in flight
+    for (; c < c1; c += st) advect_b1_cell(a, c);
 }
 
 // One sweep of the boxes of one class.  At most 256 threads per CTA; MINB
