@@ -341,21 +341,22 @@ __device__ __forceinline__ void advect_b1_cell(const AdvectArgs &a, unsigned c)
     *bp = bx;
 }
 
-// Four cells c, c + step, c + 2 step, c + 3 step at once: every load of the
-// four is issued before the first store, so a thread has twenty loads in
-// flight (the stores go to b, which the compiler cannot tell apart from the
-// flux arrays).  Same arithmetic per cell as advect_b1_cell.
-__device__ __forceinline__ void advect_b1_cell4(const AdvectArgs &a, unsigned c, unsigned step)
+// G cells c, c + step, .. at once: every load of the G is issued before the
+// first store, so a thread has 5 G loads in flight (the stores go to b, which
+// the compiler cannot tell apart from the flux arrays).  Same arithmetic per
+// cell as advect_b1_cell.
+template <int G>
+__device__ __forceinline__ void advect_b1_cells(const AdvectArgs &a, unsigned c, unsigned step)
 {
     const Frame &f = a.f;
     const int p1 = nib(f.pb, 0);
     const long long ncell = f.npen * f.n;
     (void)ncell;
-    float v[4][5];
-    float *bp[4];
-    bool ok[4];
+    float v[G][5];
+    float *bp[G];
+    bool ok[G];
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
+    for (int k = 0; k < G; ++k) {
         const unsigned ck0 = c + k * step;
         unsigned cj, ck;
         advect_b1_neighbours(a, ck0, cj, ck);
@@ -370,7 +371,7 @@ __device__ __forceinline__ void advect_b1_cell4(const AdvectArgs &a, unsigned c,
         }
     }
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
+    for (int k = 0; k < G; ++k) {
         if (!ok[k]) continue;
         float bx = fsub(v[k][0], v[k][1]);
         bx = fadd(bx, v[k][2]);

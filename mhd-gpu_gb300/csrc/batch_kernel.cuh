@@ -119,6 +119,8 @@ struct ClassWork {
 // the claim and the completion count cost little against the item's work
 constexpr int kItemCells = 2048;
 constexpr int kB1ItemCells = 4096;
+// cells of a b(1) item a thread gathers at once
+constexpr int kB1Group = 4;
 
 __device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned *p)
 {
@@ -167,7 +169,8 @@ __device__ __forceinline__ void batch_b1(const AdvectArgs &a, long long c0, int 
     const unsigned c1 = min((unsigned)c0 + (unsigned)cells, ncell);
     const unsigned st = blockDim.x;
     unsigned c = (unsigned)c0 + threadIdx.x;
-    for (; c + 3 * st < c1; c += 4 * st) advect_b1_cell4(a, c, st);   // four cells' loads in flight
+    for (; c + (kB1Group - 1) * st < c1; c += kB1Group * st)
+        advect_b1_cells<kB1Group>(a, c, st);   // kB1Group cells' loads in flight
     for (; c < c1; c += st) advect_b1_cell(a, c);
 }
 
