@@ -252,11 +252,11 @@ int mhdgpu_set_math(int mode);
 
 /* How the transpose-free step moves the pencils that run across memory (its
  * y and z sweeps) between global and shared memory:
- *   MHD_STAGING_CPASYNC (default): a full tile of the fluid and field sweeps
- *     (every row stride a multiple of 4 cells, 16-byte aligned arrays, pencils
- *     per CTA a multiple of 4) is moved as 16-byte vectors of four pencils'
- *     cells per thread; a partial tile row by row with 4-byte asynchronous
- *     copies;
+ *   MHD_STAGING_CPASYNC (default): a full tile of the fluid sweep (every row
+ *     stride a multiple of 4 cells, 16-byte aligned arrays, pencils per CTA a
+ *     multiple of 4) is moved as 16-byte vectors of four pencils' cells per
+ *     thread; partial tiles and the field sweep's tiles row by row with
+ *     4-byte asynchronous copies;
  *   MHD_STAGING_TMA: where the frame allows (pencils of 32, 64 or 128 cells in
  *     teams of one warp, 8 per CTA, every row stride a multiple of 4 cells,
  *     16-byte aligned arrays) the fluid tile is loaded and stored by tensor
