@@ -6,7 +6,7 @@ namespace mhd {
 
 template <int CPL, int WPP, class M, bool ROWS, int NT>
 __global__ void __launch_bounds__(256)
-advect_flux_kernel(AdvectArgs a)
+advect_flux_kernel(const __grid_constant__ AdvectArgs a)
 {
     advect_tile<CPL, WPP, M, ROWS, NT>(a, blockIdx.x);
 }

@@ -15,6 +15,8 @@
 // coalesced in either staging mode.
 #pragma once
 
+#include <type_traits>
+
 #include "fluidx_reg.cuh"
 
 #undef MHD_DBG_FILE
@@ -29,8 +31,8 @@ __host__ __device__ inline long long axr_smem_floats(int n, int ppc) { return 8L
 // arrays of the staging area
 enum { kAxRho = 0, kAxM = 1, kAxRhoJ = 2, kAxMJ = 3, kAxRhoK = 4, kAxMK = 5, kAxB2 = 6, kAxB3 = 7 };
 
-template <int CPL, int TPP, class M, bool ROWS>
-__device__ __forceinline__ void advect_tile_reg(const AdvectArgs &a, long long tile)
+template <int CPL, int TPP, bool ROWS, class MP>
+__device__ __forceinline__ bool advect_tile_reg_pass(const AdvectArgs &a, long long tile, MP &mp)
 {
     constexpr int N = TPP * CPL, R = N + 4;
     extern __shared__ __align__(16) float smem_r[];
@@ -142,7 +144,7 @@ __device__ __forceinline__ void advect_tile_reg(const AdvectArgs &a, long long t
             lds_run<CPL>(run + (st ? kAxMK : kAxMJ) * PR, mn);
             lds_run<CPL>(run + (st ? kAxB3 : kAxB2) * PR, bb);
 #pragma unroll
-            for (int m = 0; m < CPL; ++m) v[m] = M::div(M::add(mn[m], mo[m]), M::add(rn[m], ro[m]));
+            for (int m = 0; m < CPL; ++m) v[m] = mp.div(mp.add(mn[m], mo[m]), mp.add(rn[m], ro[m]));
         } else {
 #pragma unroll
             for (int m = 0; m < CPL; ++m) { v[m] = 0.0f; bb[m] = 0.0f; }
@@ -153,16 +155,16 @@ __device__ __forceinline__ void advect_tile_reg(const AdvectArgs &a, long long t
         float g[CPL], bg[CPL];
 #pragma unroll
         for (int m = 0; m < CPL; ++m) {
-            const float s = M::add(m > 0 ? v[m - 1] : vl, m + 1 < CPL ? v[m + 1] : vr);
-            g[m] = 0.25f * M::twice_plus(v[m], s);
-            bg[m] = M::mul(bb[m], g[m]);
+            const float s = mp.add(m > 0 ? v[m - 1] : vl, m + 1 < CPL ? v[m + 1] : vr);
+            g[m] = 0.25f * mp.twice_plus(v[m], s);
+            bg[m] = mp.mul(bb[m], g[m]);
         }
         // tvdb: vh = (vg + cshift(vg,1))/2 ; flux1 = b vg, upwinded by vh
         const float gr = ln.from(g[0], 1), bgr = ln.from(bg[0], 1);
         float h[CPL], f1[CPL];
 #pragma unroll
         for (int m = 0; m < CPL; ++m) {
-            h[m] = M::add(0.5f * g[m], 0.5f * (m + 1 < CPL ? g[m + 1] : gr));
+            h[m] = mp.add(0.5f * g[m], 0.5f * (m + 1 < CPL ? g[m + 1] : gr));
             f1[m] = (h[m] > 0.0f) ? bg[m] : (m + 1 < CPL ? bg[m + 1] : bgr);
         }
         // b1 = b - (flux1 - cshift(flux1,-1)) dt/2 (the product float, the
@@ -171,8 +173,8 @@ __device__ __forceinline__ void advect_tile_reg(const AdvectArgs &a, long long t
         float gb[CPL];
 #pragma unroll
         for (int m = 0; m < CPL; ++m) {
-            const float b1 = M::minus_half(bb[m], M::mul(M::sub(f1[m], m > 0 ? f1[m - 1] : f1l), dt));
-            gb[m] = M::mul(g[m], b1);
+            const float b1 = mp.minus_half(bb[m], mp.mul(mp.sub(f1[m], m > 0 ? f1[m - 1] : f1l), dt));
+            gb[m] = mp.mul(g[m], b1);
         }
         // upwind second-order flux on the right face with the van Leer limiter
         // (tvdb.c:64-75), from vg*b1 of cells c-1 .. c+2
@@ -184,21 +186,26 @@ __device__ __forceinline__ void advect_tile_reg(const AdvectArgs &a, long long t
         for (int m = 0; m < CPL; ++m) {
             const bool up = h[m] > 0.0f;
             const float w = up ? GB(m) : GB(m + 1);
-            const float Wp = up ? M::sub(GB(m + 1), w) : M::sub(w, GB(m + 2));
-            const float Wm = up ? M::sub(w, GB(m - 1)) : M::sub(GB(m), w);
-            const float dw = M::slope(Wm, Wp);
-            fl[m] = M::mul(M::add(w, dw), dt);
+            const float Wp = up ? mp.sub(GB(m + 1), w) : mp.sub(w, GB(m + 2));
+            const float Wm = up ? mp.sub(w, GB(m - 1)) : mp.sub(GB(m), w);
+            const float dw = mp.slope(Wm, Wp);
+            fl[m] = mp.mul(mp.add(w, dw), dt);
         }
         // b = b - (flux - cshift(flux,-1)) ; the shifted flux is kept for b(1)
         const float fll = ln.from(fl[CPL - 1], -1);
 #pragma unroll
         for (int m = 0; m < CPL; ++m) {
             const float sp = m > 0 ? fl[m - 1] : fll;
-            bout[st][m] = M::sub(bb[m], M::sub(fl[m], sp));
+            bout[st][m] = mp.sub(bb[m], mp.sub(fl[m], sp));
             sout[st][m] = sp;
         }
     }
 
+    // A flagged pass writes nothing when a lane of the CTA formed a value near
+    // a rounding boundary: its caller computes the tile again exactly.
+    if constexpr (MP::kFlagged) {
+        if (__syncthreads_or(mp.nb ? 1 : 0)) return false;
+    }
     // ---- outputs through shared memory: arrays b(2), b(3), sA, sB ----
     __syncthreads();   // the inputs are consumed
     if (live) {
@@ -243,6 +250,33 @@ __device__ __forceinline__ void advect_tile_reg(const AdvectArgs &a, long long t
                                            w < 2 ? MHD_NB(f) : f.npen * f.n))
                 dst[cell * dstride] = o[i];
         }
+    }
+    return true;
+}
+
+// the exact pass of a flagged tile, out of line: the hot code then makes no
+// call (the FP64 fallbacks' call convention would claim its registers)
+template <int CPL, int TPP, bool ROWS>
+__device__ MHD_COLD void advect_tile_reg_exact(const AdvectArgs &a, long long tile)
+{
+    Faithful m;
+    advect_tile_reg_pass<CPL, TPP, ROWS>(a, tile, m);
+}
+
+// One tile of the field sweep; Faithful runs as FaithfulNB first (see
+// fluidx_tile_reg).
+template <int CPL, int TPP, class M, bool ROWS>
+__device__ __forceinline__ void advect_tile_reg(const AdvectArgs &a, long long tile)
+{
+    if constexpr (std::is_same<M, Faithful>::value) {
+        FaithfulNB f;
+        if (!advect_tile_reg_pass<CPL, TPP, ROWS>(a, tile, f)) {
+            __syncthreads();   // the flagged pass's shared memory is consumed
+            advect_tile_reg_exact<CPL, TPP, ROWS>(a, tile);
+        }
+    } else {
+        M m;
+        advect_tile_reg_pass<CPL, TPP, ROWS>(a, tile, m);
     }
 }
 

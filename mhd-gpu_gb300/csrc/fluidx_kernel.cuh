@@ -415,7 +415,7 @@ __device__ __forceinline__ void fluidx_tile(const FluidxArgs &a, long long tile)
 
 template <int CPL, int WPP, class M, bool ROWS, int NT>
 __global__ void __launch_bounds__(256)
-fluidx_kernel(FluidxArgs a)
+fluidx_kernel(const __grid_constant__ FluidxArgs a)
 {
     fluidx_tile<CPL, WPP, M, ROWS, NT, true>(a, blockIdx.x);
 }

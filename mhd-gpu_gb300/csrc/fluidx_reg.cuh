@@ -19,6 +19,8 @@
 //  - there are no exchange rows in shared memory and no team barriers.
 #pragma once
 
+#include <type_traits>
+
 #include "kernels.cuh"
 #include "tma_rows.cuh"
 
@@ -244,8 +246,8 @@ __device__ __forceinline__ void rows_vec_writeback(const Frame &f, float *u_out,
 // single-box kernels take it, the register-capped batch kernels do not.
 // TMA: rows mode stages the tile and writes it back through tensor copies
 // (tma_rows.cuh; tm holds the frame's maps, ppc = kTmaPencils, in place).
-template <int CPL, int TPP, class M, bool ROWS, bool GROUPED = false, bool TMA = false>
-__device__ __forceinline__ void fluidx_tile_reg(const FluidxArgs &a, long long tile, const RowMaps *tm = nullptr)
+template <int CPL, int TPP, bool ROWS, bool GROUPED, bool TMA, class MP>
+__device__ __forceinline__ bool fluidx_tile_reg_pass(const FluidxArgs &a, long long tile, const RowMaps *tm, MP &mp)
 {
     constexpr int N = TPP * CPL;
     constexpr int CS = N + 4, PS = 5 * CS, BSC = 3 * N, BSR = 3 * N + 4, KS = N + 4;
@@ -444,6 +446,7 @@ __device__ __forceinline__ void fluidx_tile_reg(const FluidxArgs &a, long long t
 
     const float hdt = 0.5f * dt;
     unsigned bad = 0;
+    float cfl_c = 0.0f;   // the last x sweep: the CFL speed of the updated cells
     float u1[CPL][5];
 
     // ================= half step =================
@@ -458,7 +461,7 @@ __device__ __forceinline__ void fluidx_tile_reg(const FluidxArgs &a, long long t
             for (int m = 0; m < CPL; ++m) {
                 const float uu[5] = {uc[0][m], uc[1][m], uc[2][m], uc[3][m], uc[4][m]};
                 float cs, p;
-                cell_flux<M>(uu, bc[m], v[m], cs, p);
+                cell_flux(mp, uu, bc[m], v[m], cs, p);
                 cl = fmaxf(cl, cs);
             }
         }
@@ -466,7 +469,7 @@ __device__ __forceinline__ void fluidx_tile_reg(const FluidxArgs &a, long long t
         // v/c where c > 0 (mhdflux.c:48-57); where c = 0 the quotient by 1
         // leaves every finite v as it is, without a select per value
         const float cd = c > 0.0f ? c : 1.0f;
-        const float yc = M::recip(cd);
+        const float yc = mp.recip(cd);
 #pragma unroll
         for (int ii = 0; ii < 5; ++ii) {
             float uu[CPL], wl[CPL], fl[CPL];
@@ -474,20 +477,20 @@ __device__ __forceinline__ void fluidx_tile_reg(const FluidxArgs &a, long long t
             // fr = c(u + v/c) (kept in u1), wl = u - v/c
 #pragma unroll
             for (int m = 0; m < CPL; ++m) {
-                const float vv = M::divy(v[m][ii], cd, yc);
-                u1[m][ii] = M::mul(c, M::add(uu[m], vv));
-                wl[m] = M::sub(uu[m], vv);
+                const float vv = mp.divy(v[m][ii], cd, yc);
+                u1[m][ii] = mp.mul(c, mp.add(uu[m], vv));
+                wl[m] = mp.sub(uu[m], vv);
             }
             // flux = (fr - c*cshift(wl,+1))/2
             const float wr = ln.from(wl[0], 1);
 #pragma unroll
             for (int m = 0; m < CPL; ++m)
-                fl[m] = 0.5f * M::sub(u1[m][ii], M::mul(c, (m + 1 < CPL) ? wl[m + 1] : wr));
+                fl[m] = 0.5f * mp.sub(u1[m][ii], mp.mul(c, (m + 1 < CPL) ? wl[m + 1] : wr));
             // u1 = u - (flux - cshift(flux,-1)) dt/2
             const float fm = ln.from(fl[CPL - 1], -1);
 #pragma unroll
             for (int m = 0; m < CPL; ++m)
-                u1[m][ii] = M::add(uu[m], M::mul(-hdt, M::sub(fl[m], m > 0 ? fl[m - 1] : fm)));
+                u1[m][ii] = mp.add(uu[m], mp.mul(-hdt, mp.sub(fl[m], m > 0 ? fl[m - 1] : fm)));
         }
     }
 
@@ -498,7 +501,7 @@ __device__ __forceinline__ void fluidx_tile_reg(const FluidxArgs &a, long long t
 #pragma unroll
         for (int m = 0; m < CPL; ++m) {
             float cs, p;
-            cell_flux<M>(u1[m], bc[m], v[m], cs, p);
+            cell_flux(mp, u1[m], bc[m], v[m], cs, p);
             cl = fmaxf(cl, cs);
             if (!(p > 0.0f)) bad |= MHD_HEALTH_PRESSURE;
         }
@@ -506,7 +509,7 @@ __device__ __forceinline__ void fluidx_tile_reg(const FluidxArgs &a, long long t
         // v/c where c > 0 (mhdflux.c:48-57); where c = 0 the quotient by 1
         // leaves every finite v as it is, without a select per value
         const float cd = c > 0.0f ? c : 1.0f;
-        const float yc = M::recip(cd);
+        const float yc = mp.recip(cd);
         const float mdt = -dt;
         float ssum[CPL];
 #pragma unroll
@@ -517,9 +520,9 @@ __device__ __forceinline__ void fluidx_tile_reg(const FluidxArgs &a, long long t
             float fr[CPL], fl[CPL];
 #pragma unroll
             for (int m = 0; m < CPL; ++m) {
-                const float vv = M::divy(v[m][ii], cd, yc);
-                fr[m] = M::mul(c, M::add(u1[m][ii], vv));
-                fl[m] = M::mul(c, M::sub(u1[m][ii], vv));
+                const float vv = mp.divy(v[m][ii], cd, yc);
+                fr[m] = mp.mul(c, mp.add(u1[m][ii], vv));
+                fl[m] = mp.mul(c, mp.sub(u1[m][ii], vv));
             }
             // neighbours: fr of cells c0-1 and c0+CPL, fl of c0+CPL and c0+CPL+1
             const float frl = ln.from(fr[CPL - 1], -1);
@@ -532,10 +535,10 @@ __device__ __forceinline__ void fluidx_tile_reg(const FluidxArgs &a, long long t
             for (int i = 0; i <= CPL; ++i) {
                 const float ra = (i < CPL) ? fr[i] : frr;
                 const float rb = (i > 0) ? fr[i - 1] : frl;
-                dr[i] = M::sub(ra, rb);
+                dr[i] = mp.sub(ra, rb);
                 const float la = (i < CPL) ? fl[i] : flr1;
                 const float lb = (i + 1 < CPL) ? fl[i + 1] : (i + 1 == CPL ? flr1 : flr2);
-                dl[i] = M::sub(la, lb);
+                dl[i] = mp.sub(la, lb);
             }
             // flux = (fr - fl + dfr - dfl)/2 with van Leer slopes (tvd1.c:54-112):
             // dfr = slope(fr(c+1)-fr(c), fr(c)-fr(c-1)),
@@ -543,10 +546,10 @@ __device__ __forceinline__ void fluidx_tile_reg(const FluidxArgs &a, long long t
             float fx[CPL];
 #pragma unroll
             for (int m = 0; m < CPL; ++m) {
-                const float dfr = M::slope(dr[m + 1], dr[m]);
-                const float dfl = M::slope(dl[m + 1], dl[m]);
+                const float dfr = mp.slope(dr[m + 1], dr[m]);
+                const float dfl = mp.slope(dl[m + 1], dl[m]);
                 const float fl0 = (m + 1 < CPL) ? fl[m + 1] : flr1;
-                fx[m] = 0.5f * M::add(M::sub(fr[m], fl0), M::sub(dfr, dfl));
+                fx[m] = 0.5f * mp.add(mp.sub(fr[m], fl0), mp.sub(dfr, dfl));
             }
             // u = u - (flux - cshift(flux,-1)) dt, written back into US
             const float fxl = ln.from(fx[CPL - 1], -1);
@@ -554,7 +557,7 @@ __device__ __forceinline__ void fluidx_tile_reg(const FluidxArgs &a, long long t
             load_comp<CPL>(us + ii * CS, live, ii, uu);
 #pragma unroll
             for (int m = 0; m < CPL; ++m) {
-                un[m] = M::add(uu[m], M::mul(mdt, M::sub(fx[m], m > 0 ? fx[m - 1] : fxl)));
+                un[m] = mp.add(uu[m], mp.mul(mdt, mp.sub(fx[m], m > 0 ? fx[m - 1] : fxl)));
                 ssum[m] += un[m];
                 if (ii == 0 && !(un[m] > 0.0f)) bad |= MHD_HEALTH_DENSITY;
             }
@@ -568,7 +571,6 @@ __device__ __forceinline__ void fluidx_tile_reg(const FluidxArgs &a, long long t
         if (!ROWS && a.cfl != nullptr) {
             const float *bs = BS + q * BSC + c0 * 3;   // this run's staged b
             const float nb0 = ln.from(live && MHD_SM(bs, 4) ? bs[0] : 0.0f, 1);
-            float cfl_c = 0.0f;
             if (live) {
 #pragma unroll
                 for (int m = 0; m < CPL; ++m) {
@@ -578,7 +580,8 @@ __device__ __forceinline__ void fluidx_tile_reg(const FluidxArgs &a, long long t
                     if (!MHD_SM(bs + 3 * m, 12) || !MHD_SM(bs + 3 * (m + 1 < CPL ? m + 1 : m), 4)) continue;
                     if (a.cfl_mode == MHD_CFL_C) {
                         bb[0] = bs[3 * m]; bb[1] = bs[3 * m + 1]; bb[2] = bs[3 * m + 2];
-                        cfl_c = fmaxf(cfl_c, cfl_speed_c(um, bb));
+                        if constexpr (MP::kFlagged) cfl_c = fmaxf(cfl_c, cfl_speed_c_ff(um, bb, mp.nb));
+                        else cfl_c = fmaxf(cfl_c, cfl_speed_c(um, bb));
                     } else {
                         const float bnext = (m + 1 < CPL) ? bs[3 * (m + 1)] : nb0;
                         bb[0] = fdiv(fadd(bs[3 * m], bnext), 2.0f);
@@ -591,10 +594,16 @@ __device__ __forceinline__ void fluidx_tile_reg(const FluidxArgs &a, long long t
                     }
                 }
             }
-            cfl_warp_max(cfl_c, a.cfl);   // every lane of the warp
         }
     }
 
+    // A flagged pass commits nothing when a lane of the CTA formed a value
+    // near a rounding boundary: its caller computes the tile again exactly
+    // (the inputs are still untouched in memory).
+    if constexpr (MP::kFlagged) {
+        if (__syncthreads_or(mp.nb ? 1 : 0)) return false;
+    }
+    if (!ROWS && a.cfl != nullptr) cfl_warp_max(cfl_c, a.cfl);   // every lane of the warp
     if (!live) bad = 0;
     if (bad) flag_health(a.health, bad);
     __syncthreads();
@@ -681,6 +690,34 @@ __device__ __forceinline__ void fluidx_tile_reg(const FluidxArgs &a, long long t
                         g[lane + 32 * h] = US[off[h] + i];
             }
         }
+    }
+    return true;
+}
+
+// the exact pass of a flagged tile, out of line: the hot code then makes no
+// call (the FP64 fallbacks' call convention would claim its registers)
+template <int CPL, int TPP, bool ROWS, bool GROUPED, bool TMA>
+__device__ MHD_COLD void fluidx_tile_reg_exact(const FluidxArgs &a, long long tile, const RowMaps *tm)
+{
+    Faithful m;
+    fluidx_tile_reg_pass<CPL, TPP, ROWS, GROUPED, TMA>(a, tile, tm, m);
+}
+
+// One tile of the fluid sweep.  Faithful (the C path's rounding) runs first
+// as FaithfulNB, without its FP64 fallbacks in the hot code; the rare tile in
+// which a value lies near a rounding boundary is computed again with them.
+template <int CPL, int TPP, class M, bool ROWS, bool GROUPED = false, bool TMA = false>
+__device__ __forceinline__ void fluidx_tile_reg(const FluidxArgs &a, long long tile, const RowMaps *tm = nullptr)
+{
+    if constexpr (std::is_same<M, Faithful>::value) {
+        FaithfulNB f;
+        if (!fluidx_tile_reg_pass<CPL, TPP, ROWS, GROUPED, TMA>(a, tile, tm, f)) {
+            __syncthreads();   // the flagged pass's shared memory is consumed
+            fluidx_tile_reg_exact<CPL, TPP, ROWS, GROUPED, TMA>(a, tile, tm);
+        }
+    } else {
+        M m;
+        fluidx_tile_reg_pass<CPL, TPP, ROWS, GROUPED, TMA>(a, tile, tm, m);
     }
 }
 
