@@ -296,12 +296,12 @@ __device__ __forceinline__ void advect_tile_team(const AdvectArgs &a, long long 
 
 // One CTA's work on a tile (advect_flux_kernel, the batched kernel): pencils
 // that fill a team of at most one warp exactly take the register-blocked tile
-// (same results).
-template <int CPL, int WPP, class M, bool ROWS, int NT>
+// (same results; FLAGGED: its flagged pass, see fluidx_tile_reg).
+template <int CPL, int WPP, class M, bool ROWS, int NT, bool FLAGGED = false>
 __device__ __forceinline__ void advect_tile(const AdvectArgs &a, long long tile)
 {
     if constexpr (NT > 0 && reg_tile_shape(NT, CPL, WPP))
-        advect_tile_reg<CPL, team_threads<WPP>(), M, ROWS>(a, tile);
+        advect_tile_reg<CPL, team_threads<WPP>(), M, ROWS, FLAGGED>(a, tile);
     else
         advect_tile_team<CPL, WPP, M, ROWS, NT>(a, tile);
 }

@@ -263,12 +263,12 @@ __device__ MHD_COLD void advect_tile_reg_exact(const AdvectArgs &a, long long ti
     advect_tile_reg_pass<CPL, TPP, ROWS>(a, tile, m);
 }
 
-// One tile of the field sweep; Faithful runs as FaithfulNB first (see
-// fluidx_tile_reg).
-template <int CPL, int TPP, class M, bool ROWS>
+// One tile of the field sweep; FLAGGED (the batched kernels): Faithful runs
+// as FaithfulNB first (see fluidx_tile_reg).
+template <int CPL, int TPP, class M, bool ROWS, bool FLAGGED = false>
 __device__ __forceinline__ void advect_tile_reg(const AdvectArgs &a, long long tile)
 {
-    if constexpr (std::is_same<M, Faithful>::value) {
+    if constexpr (FLAGGED && std::is_same<M, Faithful>::value) {
         FaithfulNB f;
         if (!advect_tile_reg_pass<CPL, TPP, ROWS>(a, tile, f)) {
             __syncthreads();   // the flagged pass's shared memory is consumed

@@ -238,8 +238,8 @@ batch_class_kernel(const __grid_constant__ ClassWork w)
                 const long long t1 = min(t0 + g, batch_tiles(w.fa[bx].f, ppc, ROWS));
                 for (long long t = t0; t < t1; ++t) {
                     if (t > t0) __syncthreads();   // the previous tile's shared memory is consumed
-                    if (ph == kPhaseFluid) fluidx_tile<CPL, WPP, M, ROWS, NT>(w.fa[bx], t);
-                    else advect_tile<CPL, WPP, M, ROWS, NT>(w.aa[bx], t);
+                    if (ph == kPhaseFluid) fluidx_tile<CPL, WPP, M, ROWS, NT, false, true>(w.fa[bx], t);
+                    else advect_tile<CPL, WPP, M, ROWS, NT, true>(w.aa[bx], t);
                 }
             }
         }

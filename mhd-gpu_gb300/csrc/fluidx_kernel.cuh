@@ -403,12 +403,13 @@ __device__ __forceinline__ void fluidx_tile_team(const FluidxArgs &a, long long 
 
 // One CTA's work on a tile; called once per CTA by fluidx_kernel and in a loop
 // by the batched kernel (batch_kernel.cuh).  Pencils that fill a team of at
-// most one warp exactly take the register-blocked tile (same results).
-template <int CPL, int WPP, class M, bool ROWS, int NT, bool GROUPED = false>
+// most one warp exactly take the register-blocked tile (same results;
+// FLAGGED: its flagged pass, see fluidx_tile_reg).
+template <int CPL, int WPP, class M, bool ROWS, int NT, bool GROUPED = false, bool FLAGGED = false>
 __device__ __forceinline__ void fluidx_tile(const FluidxArgs &a, long long tile)
 {
     if constexpr (NT > 0 && reg_tile_shape(NT, CPL, WPP))
-        fluidx_tile_reg<CPL, team_threads<WPP>(), M, ROWS, GROUPED>(a, tile);
+        fluidx_tile_reg<CPL, team_threads<WPP>(), M, ROWS, GROUPED, false, FLAGGED>(a, tile);
     else
         fluidx_tile_team<CPL, WPP, M, ROWS, NT>(a, tile);
 }

@@ -703,13 +703,17 @@ __device__ MHD_COLD void fluidx_tile_reg_exact(const FluidxArgs &a, long long ti
     fluidx_tile_reg_pass<CPL, TPP, ROWS, GROUPED, TMA>(a, tile, tm, m);
 }
 
-// One tile of the fluid sweep.  Faithful (the C path's rounding) runs first
-// as FaithfulNB, without its FP64 fallbacks in the hot code; the rare tile in
-// which a value lies near a rounding boundary is computed again with them.
-template <int CPL, int TPP, class M, bool ROWS, bool GROUPED = false, bool TMA = false>
+// One tile of the fluid sweep.  FLAGGED (the batched kernels): Faithful (the
+// C path's rounding) runs first as FaithfulNB, without its FP64 fallbacks in
+// the hot code, and the rare tile in which a value lies near a rounding
+// boundary is computed again with them.  The single-box kernels call the
+// fallbacks in place: on smooth single-box states (a linear wave) the
+// near-boundary values come in whole regions and the redos cost more than
+// the calls.
+template <int CPL, int TPP, class M, bool ROWS, bool GROUPED = false, bool TMA = false, bool FLAGGED = false>
 __device__ __forceinline__ void fluidx_tile_reg(const FluidxArgs &a, long long tile, const RowMaps *tm = nullptr)
 {
-    if constexpr (std::is_same<M, Faithful>::value) {
+    if constexpr (FLAGGED && std::is_same<M, Faithful>::value) {
         FaithfulNB f;
         if (!fluidx_tile_reg_pass<CPL, TPP, ROWS, GROUPED, TMA>(a, tile, tm, f)) {
             __syncthreads();   // the flagged pass's shared memory is consumed
