@@ -254,10 +254,10 @@ __device__ __forceinline__ bool advect_tile_reg_pass(const AdvectArgs &a, long l
     return true;
 }
 
-// the exact pass of a flagged tile, out of line: the hot code then makes no
-// call (the FP64 fallbacks' call convention would claim its registers)
+// the exact pass of a flagged tile, after the flagged pass (see
+// fluidx_tile_reg_exact)
 template <int CPL, int TPP, bool ROWS>
-__device__ MHD_COLD void advect_tile_reg_exact(const AdvectArgs &a, long long tile)
+__device__ __forceinline__ void advect_tile_reg_exact(const AdvectArgs &a, long long tile)
 {
     Faithful m;
     advect_tile_reg_pass<CPL, TPP, ROWS>(a, tile, m);

@@ -694,10 +694,11 @@ __device__ __forceinline__ bool fluidx_tile_reg_pass(const FluidxArgs &a, long l
     return true;
 }
 
-// the exact pass of a flagged tile, out of line: the hot code then makes no
-// call (the FP64 fallbacks' call convention would claim its registers)
+// the exact pass of a flagged tile, after the flagged pass: its FP64
+// fallbacks' calls sit outside the flagged pass's hot code (inlined: out of
+// line, as a call of its own, it measured 0.5 % slower on the batched step)
 template <int CPL, int TPP, bool ROWS, bool GROUPED, bool TMA>
-__device__ MHD_COLD void fluidx_tile_reg_exact(const FluidxArgs &a, long long tile, const RowMaps *tm)
+__device__ __forceinline__ void fluidx_tile_reg_exact(const FluidxArgs &a, long long tile, const RowMaps *tm)
 {
     Faithful m;
     fluidx_tile_reg_pass<CPL, TPP, ROWS, GROUPED, TMA>(a, tile, tm, m);

@@ -20,16 +20,6 @@
 #define MHD_HD inline
 #endif
 
-// The exact pass of a flagged tile is out of line, so that the hot code makes
-// no call.  Under -rdc (the debug build) an out-of-line function has its own
-// register count, which the batch kernels' launch bounds do not cap: there it
-// is inlined.
-#if defined(MHD_DEBUG)
-#define MHD_COLD __forceinline__
-#else
-#define MHD_COLD __noinline__
-#endif
-
 namespace mhd {
 
 constexpr float kGamma = 1.66666662693023681640625f;     // (float)(5.0/3.0)
